@@ -1,0 +1,237 @@
+"""GB300 (sm_103a) batched block-tridiagonal SPD solver.
+
+Python mirror of BlockStructuredSolvers.jl's GPU API (src/BlockStructuredSolvers.jl:9-11
+exports) over the C ABI of ``libbss_gb300.so`` (``include/bss.h``):
+
+    data = initialize_batched(N, n, torch.float64)   # initialize_batched(N, n, T, CuArray)
+    data.A_tensor.copy_(A); data.B_tensor.copy_(B); data.d_tensor.copy_(d)
+    factorize_(data)                                  # factorize!(data)
+    solve_(data)                                      # solve!(data): d_tensor <- x
+
+``A_tensor`` (n x n x N), ``B_tensor`` (n x n x (N-1)) and ``d_tensor``
+(n x k x N) are torch views of library-owned device memory with Julia's
+column-major strides, so ``data.A_tensor[:, :, i]`` is the block A_i exactly
+as ``data.A_tensor[:, :, i]`` is in Julia, and ``A_list[i]`` aliases it.
+
+All compute runs in the sm_103a kernels of the library; there is no CPU or
+PyTorch fallback.  Loading fails loudly if the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+
+from . import _lib
+from ._lib import BSSError, NotSPDError  # noqa: F401
+
+__all__ = [
+    "BlockTriDiagData_batched", "BlockTriDiagData_seq", "initialize_batched", "initialize_seq",
+    "factorize_", "solve_", "factorize", "solve", "synchronize", "get_info", "residual",
+    "plan_reference", "BSSError", "NotSPDError",
+]
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _dtype_code(T):
+    torch = _torch()
+    if T in (torch.float64, "float64", "Float64", "f64", float):
+        return _lib.BSS_F64, torch.float64
+    if T in (torch.float32, "float32", "Float32", "f32"):
+        return _lib.BSS_F32, torch.float32
+    raise ValueError(f"unsupported element type {T!r}: Float32 or Float64")
+
+
+class _DevView:
+    """__cuda_array_interface__ over library memory; keeps the owner alive."""
+
+    def __init__(self, ptr, shape, strides, typestr, owner):
+        self._owner = owner
+        self.__cuda_array_interface__ = {
+            "shape": tuple(int(s) for s in shape),
+            "strides": tuple(int(s) for s in strides),
+            "typestr": typestr,
+            "data": (int(ptr), False),
+            "version": 3,
+            "stream": None,
+        }
+
+
+class _Handle:
+    """Owns a bss_handle*; destroyed when the last tensor view is gone."""
+
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                _lib.load().bss_destroy(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+
+class _Data:
+    def __init__(self, handle: _Handle, torch_dtype, N_user: int):
+        torch = _torch()
+        L = _lib.load()
+        self._h = handle
+        N = ctypes.c_int64()
+        n = ctypes.c_int64()
+        k = ctypes.c_int64()
+        dt = ctypes.c_int32()
+        _lib.check(L.bss_get_dims(handle.ptr, ctypes.byref(N), ctypes.byref(n), ctypes.byref(k),
+                                  ctypes.byref(dt)))
+        A = ctypes.c_void_p()
+        B = ctypes.c_void_p()
+        d = ctypes.c_void_p()
+        _lib.check(L.bss_get_tensors(handle.ptr, ctypes.byref(A), ctypes.byref(B), ctypes.byref(d)))
+        self.N = N.value
+        self.n = n.value
+        self.k = k.value
+        self.N_user = N_user
+        self.dtype = torch_dtype
+        es = 8 if torch_dtype == torch.float64 else 4
+        ts = "<f8" if es == 8 else "<f4"
+        nn = self.n * self.n
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self.A_tensor = torch.as_tensor(
+            _DevView(A.value, (self.n, self.n, self.N), (es, es * self.n, es * nn), ts, handle), device=dev)
+        self.B_tensor = torch.as_tensor(
+            _DevView(B.value, (self.n, self.n, max(self.N - 1, 0)), (es, es * self.n, es * nn), ts, handle),
+            device=dev)
+        self.d_tensor = torch.as_tensor(
+            _DevView(d.value, (self.n, self.k, self.N), (es, es * self.n, es * self.n * self.k), ts, handle),
+            device=dev)
+        self.A_list = [self.A_tensor[:, :, i] for i in range(self.N)]
+        self.B_list = [self.B_tensor[:, :, i] for i in range(max(self.N - 1, 0))]
+        self.d_list = [self.d_tensor[:, :, i] for i in range(self.N)]
+
+    @property
+    def handle(self):
+        return self._h.ptr
+
+
+class BlockTriDiagData_batched(_Data):
+    """``BlockTriDiagData_batched`` (src/gpu_batched.jl:1-71): N (padded N_use),
+    n, A_tensor, B_tensor, d_tensor and the per-block lists.  The per-level
+    workspace of the reference struct lives inside the library handle."""
+
+
+class BlockTriDiagData_seq(_Data):
+    """``BlockTriDiagData_seq`` (src/gpu_seq.jl:1-27)."""
+
+
+def _stream_ptr(stream):
+    torch = _torch()
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(int(stream.cuda_stream))
+
+
+def initialize_batched(N: int, n: int, T=None, M=None, *, k: int = 1, precision: str = "plain",
+                       plan: str = "auto", max_refine: int = 10, tol: float = 1e-12,
+                       target_partitions: int = 0, seq_cutoff: int = 0, stream=None
+                       ) -> BlockTriDiagData_batched:
+    """initialize_batched(N, n, T, CuArray) (src/gpu_batched.jl:165-182).
+
+    ``M`` is accepted for signature parity (the reference passes CuArray) and
+    ignored.  ``precision="mixed"`` (Float64 only): FP32 factorization with
+    FP64 iterative refinement to ``tol``.  ``plan="reference"`` uses the
+    reference planner's level sequence; "auto" sizes partitions to the GPU.
+    """
+    torch = _torch()
+    code, tdt = _dtype_code(torch.float64 if T is None else T)
+    o = _lib.default_options()
+    o.precision = {"plain": _lib.BSS_PRECISION_PLAIN, "mixed": _lib.BSS_PRECISION_MIXED}[precision]
+    o.plan = {"auto": _lib.BSS_PLAN_AUTO, "reference": _lib.BSS_PLAN_REFERENCE}[plan]
+    o.max_refine = int(max_refine)
+    o.tol = float(tol)
+    o.target_partitions = int(target_partitions)
+    o.seq_cutoff = int(seq_cutoff)
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    torch.cuda.current_device()  # make torch bind the device's primary context first
+    _lib.check(L.bss_create_batched(int(N), int(n), int(k), code, _stream_ptr(stream), ctypes.byref(o),
+                                    ctypes.byref(h)))
+    return BlockTriDiagData_batched(_Handle(h.value), tdt, int(N))
+
+
+def initialize_seq(N: int, n: int, T=None, M=None, *, k: int = 1, stream=None) -> BlockTriDiagData_seq:
+    """initialize_seq(N, n, T, CuArray) (src/gpu_seq.jl:45-59)."""
+    torch = _torch()
+    code, tdt = _dtype_code(torch.float64 if T is None else T)
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    torch.cuda.current_device()
+    _lib.check(L.bss_create_seq(int(N), int(n), int(k), code, _stream_ptr(stream), ctypes.byref(h)))
+    return BlockTriDiagData_seq(_Handle(h.value), tdt, int(N))
+
+
+def factorize_(data: _Data, check: bool = False) -> None:
+    """factorize!(data) (src/gpu_batched.jl:184-227 / src/gpu_seq.jl:61-71).
+    Asynchronous on the handle's stream; ``check=True`` waits and raises
+    NotSPDError if a pivot failed."""
+    _lib.check(_lib.load().bss_factorize(data.handle))
+    if check:
+        synchronize(data)
+
+
+def solve_(data: _Data, check: bool = False) -> None:
+    """solve!(data) (src/gpu_batched.jl:229-258 / src/gpu_seq.jl:73-84):
+    d_tensor <- A^{-1} d_tensor."""
+    _lib.check(_lib.load().bss_solve(data.handle))
+    if check:
+        synchronize(data)
+
+
+factorize = factorize_
+solve = solve_
+
+
+def synchronize(data: _Data) -> None:
+    """Wait for the handle's stream; raise on a failed pivot or on a
+    refinement that missed its tolerance."""
+    _lib.check(_lib.load().bss_synchronize(data.handle))
+
+
+def get_info(data: _Data) -> dict:
+    inf = _lib.Info()
+    _lib.check(_lib.load().bss_get_info(data.handle, ctypes.byref(inf)))
+    return {k: getattr(inf, k) for k, _ in _lib.Info._fields_}
+
+
+def residual(A_tensor, B_tensor, x_tensor, d_tensor, stream=None) -> float:
+    """||d - T x||_inf / (||T||_inf ||x||_inf + ||d||_inf) on the device (FP64
+    accumulation) for column-major (n,n,N)/(n,n,N-1)/(n,k,N) tensors."""
+    torch = _torch()
+    n, _, N = A_tensor.shape
+    k = x_tensor.shape[1]
+    code, _ = _dtype_code(A_tensor.dtype)
+
+    def colmajor(t):
+        return t.stride(0) == 1 and t.stride(1) == t.shape[0] and t.stride(2) == t.shape[0] * t.shape[1]
+
+    for t in (A_tensor, x_tensor, d_tensor):
+        if not colmajor(t) or not t.is_cuda:
+            raise ValueError("tensors must be column-major CUDA tensors")
+    out = ctypes.c_double()
+    Bp = B_tensor.data_ptr() if B_tensor.numel() else A_tensor.data_ptr()
+    _lib.check(_lib.load().bss_residual(N, n, k, code, ctypes.c_void_p(A_tensor.data_ptr()), ctypes.c_void_p(Bp),
+                                        ctypes.c_void_p(x_tensor.data_ptr()), ctypes.c_void_p(d_tensor.data_ptr()),
+                                        _stream_ptr(stream), ctypes.byref(out)))
+    return out.value
+
+
+def plan_reference(N: int):
+    return _lib.plan_reference(N)
+
+
+def colmajor_empty(shape, dtype, device="cuda"):
+    """A torch tensor with Julia column-major strides (shape (r, c, N))."""
+    torch = _torch()
+    r, c, N = shape
+    return torch.empty((N, c, r), dtype=dtype, device=device).permute(2, 1, 0)

@@ -1,0 +1,139 @@
+"""ctypes binding of the C ABI declared in ``include/bss.h``.
+
+The library is the in-tree ``libbss_gb300.so`` built by ``build.py`` for
+sm_103a.  There is no fallback: if the library is missing or fails to load,
+``load()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbss_gb300.so")
+
+BSS_OK = 0
+BSS_ERR_ARG = 1
+BSS_ERR_OOM = 2
+BSS_ERR_CUDA = 3
+BSS_ERR_NOT_SPD = 4
+BSS_ERR_TIMEOUT = 5
+BSS_ERR_UNSUPPORTED = 6
+BSS_ERR_STATE = 7
+BSS_ERR_NOT_CONVERGED = 8
+
+BSS_F32 = 0
+BSS_F64 = 1
+BSS_PRECISION_PLAIN = 0
+BSS_PRECISION_MIXED = 1
+BSS_PLAN_AUTO = 0
+BSS_PLAN_REFERENCE = 1
+
+# every entry point include/bss.h declares
+EXPORTS = (
+    "bss_default_options", "bss_create_batched", "bss_create_seq", "bss_destroy",
+    "bss_get_tensors", "bss_get_dims", "bss_factorize", "bss_solve", "bss_synchronize",
+    "bss_get_info", "bss_last_error_string", "bss_plan_reference", "bss_residual",
+    "bss_factorize_levels", "bss_get_level", "bss_version",
+)
+
+
+class Options(ctypes.Structure):
+    _fields_ = [
+        ("precision", ctypes.c_int32),
+        ("plan", ctypes.c_int32),
+        ("max_refine", ctypes.c_int32),
+        ("target_partitions", ctypes.c_int32),
+        ("seq_cutoff", ctypes.c_int32),
+        ("use_graphs", ctypes.c_int32),
+        ("tol", ctypes.c_double),
+    ]
+
+
+class Info(ctypes.Structure):
+    _fields_ = [
+        ("failed_block", ctypes.c_int64),
+        ("failed_level", ctypes.c_int32),
+        ("refine_steps", ctypes.c_int32),
+        ("rel_residual", ctypes.c_double),
+        ("levels", ctypes.c_int32),
+        ("coarsest_blocks", ctypes.c_int64),
+    ]
+
+
+class BSSError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[bss error {code}] {msg}")
+        self.code = code
+
+
+class NotSPDError(BSSError):
+    pass
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load libbss_gb300.so (raises OSError when it is not built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OSError(f"{p} not found: run blockstructuredsolvers_gb300/build.py (or __graft_entry__.build())")
+    L = ctypes.CDLL(p)
+    vp = ctypes.c_void_p
+    i64 = ctypes.c_int64
+    i32 = ctypes.c_int32
+    L.bss_default_options.argtypes = [ctypes.POINTER(Options)]
+    L.bss_default_options.restype = None
+    L.bss_create_batched.argtypes = [i64, i64, i64, i32, vp, ctypes.POINTER(Options), ctypes.POINTER(vp)]
+    L.bss_create_seq.argtypes = [i64, i64, i64, i32, vp, ctypes.POINTER(vp)]
+    L.bss_destroy.argtypes = [vp]
+    L.bss_get_tensors.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    L.bss_get_dims.argtypes = [vp, ctypes.POINTER(i64), ctypes.POINTER(i64), ctypes.POINTER(i64),
+                               ctypes.POINTER(i32)]
+    L.bss_factorize.argtypes = [vp]
+    L.bss_solve.argtypes = [vp]
+    L.bss_synchronize.argtypes = [vp]
+    L.bss_get_info.argtypes = [vp, ctypes.POINTER(Info)]
+    L.bss_last_error_string.argtypes = []
+    L.bss_last_error_string.restype = ctypes.c_char_p
+    L.bss_plan_reference.argtypes = [i64, ctypes.POINTER(i64), i32, ctypes.POINTER(i32), ctypes.POINTER(i64)]
+    L.bss_residual.argtypes = [i64, i64, i64, i32, vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_double)]
+    L.bss_factorize_levels.argtypes = [vp, i32]
+    L.bss_get_level.argtypes = [vp, i32, ctypes.POINTER(i64), ctypes.POINTER(i64), ctypes.POINTER(vp),
+                                ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(i32)]
+    L.bss_version.argtypes = []
+    L.bss_version.restype = ctypes.c_char_p
+    for name in EXPORTS:
+        if name not in ("bss_default_options", "bss_last_error_string", "bss_version"):
+            getattr(L, name).restype = ctypes.c_int
+    if path is None:
+        _lib = L
+    return L
+
+
+def check(code: int) -> None:
+    if code != BSS_OK:
+        msg = load().bss_last_error_string().decode(errors="replace")
+        if code == BSS_ERR_NOT_SPD:
+            raise NotSPDError(code, msg)
+        raise BSSError(code, msg)
+
+
+def default_options() -> Options:
+    o = Options()
+    load().bss_default_options(ctypes.byref(o))
+    return o
+
+
+def plan_reference(N: int):
+    """bss_plan_reference -> ([(N_l, m_l, P_l) finest first], coarsest)."""
+    L = load()
+    buf = (ctypes.c_int64 * 192)()
+    nlev = ctypes.c_int32()
+    coarse = ctypes.c_int64()
+    check(L.bss_plan_reference(int(N), buf, 64, ctypes.byref(nlev), ctypes.byref(coarse)))
+    return [(buf[3 * i], buf[3 * i + 1], buf[3 * i + 2]) for i in range(nlev.value)], coarse.value

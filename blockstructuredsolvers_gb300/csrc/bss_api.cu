@@ -1,0 +1,772 @@
+// C-ABI host side of the GB300 batched block-tridiagonal SPD solver.
+//
+// Mirrors BlockStructuredSolvers.jl's batched GPU solver
+//   initialize_batched  (src/gpu_batched.jl:165-182)  -> bss_create_batched
+//   factorize!          (src/gpu_batched.jl:184-227)  -> bss_factorize
+//   solve!              (src/gpu_batched.jl:229-258)  -> bss_solve
+//   initialize_seq/...  (src/gpu_seq.jl:45-84)        -> bss_create_seq
+// with library-owned device tensors in the reference's column-major layouts.
+//
+// Every level of the recursion lives in one device arena allocated at
+// create time; factorize/solve only launch kernels (no allocation, no host
+// round trip except one scalar per refinement step in mixed precision).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bss.h"
+#include "bss_launch.h"
+
+using namespace bss;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    return fail(e == cudaErrorMemoryAllocation ? BSS_ERR_OOM : BSS_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define BSS_CUDA(call)                                       \
+    do {                                                     \
+        cudaError_t e__ = (call);                            \
+        if (e__ != cudaSuccess) return cuda_fail(e__, #call); \
+    } while (0)
+
+enum Ty { F32 = 0, F64 = 1 };
+
+inline size_t tsize(int t) { return t == F64 ? 8 : 4; }
+
+// one level of the recursion (finest = 0; the last one is the sequential
+// coarsest level)
+struct Level {
+    long long N = 0;
+    long long Q = 0;  // partitions (0 for the sequential level)
+    bool seq = false;
+    int tin = F64;    // dtype of A/B as read by the factor kernel
+    int t = F64;      // dtype of factors, workspace and RHS at this level
+    void *A = nullptr, *B = nullptr;    // level system (input)
+    void *Af = nullptr, *Bf = nullptr;  // factor storage (== A/B when in place)
+    void *d = nullptr;                  // level RHS (t), n x k per block
+    void *Y = nullptr, *C = nullptr, *bvec = nullptr;
+};
+
+}  // namespace
+
+struct bss_handle {
+    long long N_user = 0, N = 0, n = 0, k = 0;
+    int dtype = F64;
+    bss_options opt{};
+    bool seq_api = false;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    char *arena = nullptr;
+    size_t arena_bytes = 0;
+    void *A = nullptr, *B = nullptr, *d = nullptr;  // user-visible tensors
+    std::vector<Level> levels;
+    // mixed precision workspace
+    void *c0 = nullptr;     // level-0 correction RHS (levels[0].t)
+    double *x64 = nullptr;  // FP64 solution accumulator
+    DevStatus *st = nullptr;
+    DevStatus *h_st = nullptr;  // pinned mirror
+    bool factored = false;
+    int kc_max = 1;
+    bss_info info{};
+    int sticky = BSS_OK;
+};
+
+extern "C" void bss_default_options(bss_options *o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->precision = BSS_PRECISION_PLAIN;
+    o->plan = BSS_PLAN_AUTO;
+    o->max_refine = 10;
+    o->target_partitions = 0;
+    o->seq_cutoff = 0;
+    o->use_graphs = 1;
+    o->tol = 1e-12;
+}
+
+extern "C" const char *bss_last_error_string(void) { return g_last_error.c_str(); }
+
+extern "C" const char *bss_version(void)
+{
+    return "bss-gb300 0.1 (sm_103a; fused chain kernels n<=64; FP32/FP64/mixed)";
+}
+
+// ---------------------------------------------------------------------------
+// planners
+// ---------------------------------------------------------------------------
+// _build_sequence (reference src/gpu_batched.jl:112-143): finest-first list of
+// (N_l, m_l, P_l); empty when no valid level exists.
+static void build_sequence(long long start, std::vector<long long> &Nl, std::vector<long long> &ml,
+                           std::vector<long long> &Pl)
+{
+    Nl.clear();
+    ml.clear();
+    Pl.clear();
+    long long ncur = start;
+    for (;;) {
+        long long best_m = -1, best_P = -1, backup_m = -1, backup_P = -1;
+        const long long max_m = (ncur - 3) / 2;  // C++ truncation == Julia ÷
+        for (long long m = 3; m <= max_m; ++m) {
+            const long long num = ncur + m, den = m + 1;
+            if (num % den == 0) {
+                const long long pprev = num / den;
+                if (pprev >= 3) {
+                    if (m < pprev) {
+                        best_m = m;
+                        best_P = pprev;
+                        break;
+                    } else if (backup_m < 0) {
+                        backup_m = m;
+                        backup_P = pprev;
+                    }
+                }
+            }
+        }
+        if (best_m < 0 && backup_m >= 0) {
+            best_m = backup_m;
+            best_P = backup_P;
+        }
+        if (best_m < 0) break;
+        Nl.push_back(ncur);
+        ml.push_back(best_m);
+        Pl.push_back(best_P);
+        ncur = best_P;
+    }
+}
+
+// find_sequence_upper (gpu_batched.jl:155-162)
+static void find_sequence_upper(long long N, std::vector<long long> &Nl, std::vector<long long> &ml,
+                                std::vector<long long> &Pl)
+{
+    long long nuse = N;
+    for (;;) {
+        build_sequence(nuse, Nl, ml, Pl);
+        if (!Nl.empty()) return;
+        ++nuse;
+    }
+}
+
+extern "C" int bss_plan_reference(int64_t N, int64_t *levels, int32_t maxlev, int32_t *nlev, int64_t *coarsest)
+{
+    if (N < 1 || !nlev || !coarsest) return fail(BSS_ERR_ARG, "bss_plan_reference: bad argument");
+    std::vector<long long> Nl, ml, Pl;
+    find_sequence_upper(N, Nl, ml, Pl);
+    const int L = (int)Nl.size();
+    *nlev = L;
+    *coarsest = Pl.back();
+    if (levels)
+        for (int l = 0; l < L && l < maxlev; ++l) {
+            levels[3 * l] = Nl[l];
+            levels[3 * l + 1] = ml[l];
+            levels[3 * l + 2] = Pl[l];
+        }
+    return BSS_OK;
+}
+
+// partition plan of this library: one CTA per partition, partitions sized to
+// fill the resident CTA slots of the GPU once (a chain is latency-bound, so
+// more partitions than slots only lengthens the next level), then halving
+// levels down to a short sequential chain.
+static void plan_auto(long long N, long long target, long long cutoff, std::vector<long long> &Ns,
+                      std::vector<long long> &Qs, long long &coarsest)
+{
+    Ns.clear();
+    Qs.clear();
+    long long ncur = N;
+    while (ncur > cutoff) {
+        const long long qmax = (ncur - 1) / 2;  // every partition keeps >= 1 interior block
+        long long q = std::min(target, qmax);
+        if (q < 1) break;
+        Ns.push_back(ncur);
+        Qs.push_back(q);
+        ncur = q + 1;
+    }
+    coarsest = ncur;
+}
+
+// ---------------------------------------------------------------------------
+// creation
+// ---------------------------------------------------------------------------
+namespace {
+
+struct ArenaPlan {
+    size_t bytes = 0;
+    size_t take(size_t b)
+    {
+        size_t off = bytes;
+        bytes += (b + 255) & ~(size_t)255;
+        return off;
+    }
+};
+
+int chain_ctas_per_sm(int tin, int t, int n)
+{
+    if (tin == F64 && t == F32) return chain_factor_ctas_per_sm<double, float>(n);
+    if (t == F32) return chain_factor_ctas_per_sm<float, float>(n);
+    return chain_factor_ctas_per_sm<double, double>(n);
+}
+
+int build_handle(bss_handle *h)
+{
+    const long long n = h->n, k = h->k, nn = n * n;
+    const bool mixed = h->opt.precision == BSS_PRECISION_MIXED;
+    const int D = h->dtype;
+    std::vector<long long> Ns, Qs;
+    long long coarsest = h->N;
+    if (!h->seq_api) {
+        if (h->opt.plan == BSS_PLAN_REFERENCE) {
+            std::vector<long long> Nl, ml, Pl;
+            find_sequence_upper(h->N_user, Nl, ml, Pl);  // finest first
+            for (size_t l = 0; l < Nl.size(); ++l) {
+                Ns.push_back(Nl[l]);
+                Qs.push_back(Pl[l] - 1);
+            }
+            coarsest = Pl.back();
+        } else {
+            int sms = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+            const int t0 = mixed ? F32 : D;
+            const int tin0 = D;
+            long long target = h->opt.target_partitions > 0
+                                   ? h->opt.target_partitions
+                                   : (long long)sms * chain_ctas_per_sm(tin0, t0, (int)n);
+            long long cutoff = h->opt.seq_cutoff > 0 ? h->opt.seq_cutoff : 8;
+            plan_auto(h->N, target, cutoff, Ns, Qs, coarsest);
+        }
+    }
+    // level list
+    h->levels.clear();
+    for (size_t l = 0; l < Ns.size(); ++l) {
+        Level L;
+        L.N = Ns[l];
+        L.Q = Qs[l];
+        L.seq = false;
+        L.t = mixed ? F32 : D;
+        L.tin = (l == 0) ? D : L.t;
+        h->levels.push_back(L);
+    }
+    {
+        Level L;
+        L.N = coarsest;
+        L.Q = 0;
+        L.seq = true;
+        L.t = D;  // plain: the tensor dtype; mixed: FP64 coarsest Cholesky
+        L.tin = D;
+        h->levels.push_back(L);
+    }
+    const int nlev = (int)h->levels.size();
+
+    // arena layout
+    ArenaPlan ap;
+    const size_t offA = ap.take((size_t)h->N * nn * tsize(D));
+    const size_t offB = ap.take((size_t)std::max(h->N - 1, 1LL) * nn * tsize(D));
+    const size_t offd = ap.take((size_t)h->N * n * k * tsize(D));
+    std::vector<size_t> oA(nlev), oB(nlev), od(nlev), oAf(nlev), oBf(nlev), oY(nlev), oC(nlev), ob(nlev);
+    for (int l = 0; l < nlev; ++l) {
+        Level &L = h->levels[l];
+        const size_t ts = tsize(L.t);
+        if (l > 0) {
+            oA[l] = ap.take((size_t)L.N * nn * ts);
+            oB[l] = ap.take((size_t)std::max(L.N - 1, 1LL) * nn * ts);
+            od[l] = ap.take((size_t)L.N * n * k * ts);
+        }
+        const bool separate_factor = (l == 0) && (mixed);
+        if (separate_factor) {
+            oAf[l] = ap.take((size_t)L.N * nn * ts);
+            oBf[l] = ap.take((size_t)std::max(L.N - 1, 1LL) * nn * ts);
+        }
+        if (!L.seq) {
+            oY[l] = ap.take((size_t)L.N * nn * ts);
+            oC[l] = ap.take((size_t)L.Q * 3 * nn * ts);
+            ob[l] = ap.take((size_t)L.Q * 2 * n * std::max(1LL, (long long)h->kc_max) * ts);
+        }
+    }
+    size_t oc0 = 0, ox = 0;
+    if (mixed) {
+        oc0 = ap.take((size_t)h->N * n * k * tsize(h->levels[0].t));
+        ox = ap.take((size_t)h->N * n * k * 8);
+    }
+    const size_t ost = ap.take(sizeof(DevStatus));
+    h->arena_bytes = ap.bytes;
+    cudaError_t e = cudaMalloc((void **)&h->arena, h->arena_bytes);
+    if (e != cudaSuccess) {
+        h->arena = nullptr;
+        return cuda_fail(e, "cudaMalloc(arena)");
+    }
+    char *base = h->arena;
+    BSS_CUDA(cudaMemsetAsync(base, 0, h->arena_bytes, h->stream));
+    h->A = base + offA;
+    h->B = base + offB;
+    h->d = base + offd;
+    for (int l = 0; l < nlev; ++l) {
+        Level &L = h->levels[l];
+        if (l == 0) {
+            L.A = h->A;
+            L.B = h->B;
+        } else {
+            L.A = base + oA[l];
+            L.B = base + oB[l];
+            L.d = base + od[l];
+        }
+        if ((l == 0) && mixed) {
+            L.Af = base + oAf[l];
+            L.Bf = base + oBf[l];
+        } else {
+            L.Af = L.A;
+            L.Bf = L.B;
+        }
+        if (!L.seq) {
+            L.Y = base + oY[l];
+            L.C = base + oC[l];
+            L.bvec = base + ob[l];
+        }
+    }
+    if (mixed) {
+        h->c0 = base + oc0;
+        h->x64 = reinterpret_cast<double *>(base + ox);
+        h->levels[0].d = h->c0;
+    } else {
+        h->levels[0].d = h->d;
+    }
+    h->st = reinterpret_cast<DevStatus *>(base + ost);
+    BSS_CUDA(cudaMallocHost((void **)&h->h_st, sizeof(DevStatus)));
+    std::memset(h->h_st, 0, sizeof(DevStatus));
+    // identity padding of A (gpu_batched.jl:177-179: blocks N..N_use, 1-based)
+    if (!h->seq_api) {
+        const long long first = h->N_user - 1;
+        cudaError_t ie = (D == F64)
+                             ? launch_init_identity<double>((double *)h->A, first, h->N, (int)n, h->stream)
+                             : launch_init_identity<float>((float *)h->A, first, h->N, (int)n, h->stream);
+        if (ie != cudaSuccess) return cuda_fail(ie, "init_identity");
+    }
+    h->info.failed_block = -1;
+    h->info.failed_level = -1;
+    h->info.rel_residual = -1.0;
+    h->info.levels = nlev - 1;
+    h->info.coarsest_blocks = coarsest;
+    return BSS_OK;
+}
+
+int check_dims(int64_t N, int64_t n, int64_t k, int32_t dtype)
+{
+    if (N < 1 || n < 1 || k < 1) return fail(BSS_ERR_ARG, "N, n and k must be >= 1");
+    if (dtype != BSS_F32 && dtype != BSS_F64) return fail(BSS_ERR_ARG, "dtype must be BSS_F32 or BSS_F64");
+    if (tile_for((int)n) == 0)
+        return fail(BSS_ERR_UNSUPPORTED, "block size n=" + std::to_string(n) + " exceeds the fused-kernel limit " +
+                                             std::to_string(MAX_FUSED_N));
+    return BSS_OK;
+}
+
+int create_common(bss_handle *h, int64_t N, int64_t n, int64_t k, int32_t dtype, void *stream, bss_handle **out)
+{
+    h->n = n;
+    h->k = k;
+    h->dtype = dtype;
+    h->stream = (cudaStream_t)stream;
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e != cudaSuccess) {
+        delete h;
+        return cuda_fail(e, "cudaGetDevice");
+    }
+    h->kc_max = solve_kc_max((int)n, (int)k, (int)tsize(dtype));
+    int rc = build_handle(h);
+    if (rc != BSS_OK) {
+        if (h->arena) cudaFree(h->arena);
+        if (h->h_st) cudaFreeHost(h->h_st);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return BSS_OK;
+}
+
+}  // namespace
+
+extern "C" int bss_create_batched(int64_t N, int64_t n, int64_t k, int32_t dtype, void *stream,
+                                  const bss_options *opt, bss_handle **out)
+{
+    if (!out) return fail(BSS_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    int rc = check_dims(N, n, k, dtype);
+    if (rc) return rc;
+    bss_handle *h = new bss_handle();
+    if (opt)
+        h->opt = *opt;
+    else
+        bss_default_options(&h->opt);
+    if (h->opt.precision == BSS_PRECISION_MIXED && dtype != BSS_F64) {
+        delete h;
+        return fail(BSS_ERR_ARG, "mixed precision needs FP64 tensors");
+    }
+    if (h->opt.max_refine < 0) h->opt.max_refine = 0;
+    h->N_user = N;
+    std::vector<long long> Nl, ml, Pl;
+    find_sequence_upper(N, Nl, ml, Pl);
+    h->N = Nl.front();  // N_use (the finest level of the reference plan)
+    return create_common(h, N, n, k, dtype, stream, out);
+}
+
+extern "C" int bss_create_seq(int64_t N, int64_t n, int64_t k, int32_t dtype, void *stream, bss_handle **out)
+{
+    if (!out) return fail(BSS_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    int rc = check_dims(N, n, k, dtype);
+    if (rc) return rc;
+    bss_handle *h = new bss_handle();
+    bss_default_options(&h->opt);
+    h->seq_api = true;
+    h->N_user = N;
+    h->N = N;
+    return create_common(h, N, n, k, dtype, stream, out);
+}
+
+extern "C" int bss_destroy(bss_handle *h)
+{
+    if (!h) return BSS_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    else cudaDeviceSynchronize();
+    if (h->arena) cudaFree(h->arena);
+    if (h->h_st) cudaFreeHost(h->h_st);
+    delete h;
+    return BSS_OK;
+}
+
+extern "C" int bss_get_tensors(bss_handle *h, void **A, void **B, void **d)
+{
+    if (!h) return fail(BSS_ERR_ARG, "handle is NULL");
+    if (A) *A = h->A;
+    if (B) *B = h->B;
+    if (d) *d = h->d;
+    return BSS_OK;
+}
+
+extern "C" int bss_get_dims(bss_handle *h, int64_t *N, int64_t *n, int64_t *k, int32_t *dtype)
+{
+    if (!h) return fail(BSS_ERR_ARG, "handle is NULL");
+    if (N) *N = h->N;
+    if (n) *n = h->n;
+    if (k) *k = h->k;
+    if (dtype) *dtype = h->dtype;
+    return BSS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// factorize
+// ---------------------------------------------------------------------------
+namespace {
+
+template <class Tin, class T>
+cudaError_t factor_level(bss_handle *h, int l)
+{
+    Level &L = h->levels[l];
+    ChainFactorArgs<Tin, T> a;
+    a.A_in = (const Tin *)L.A;
+    a.B_in = (const Tin *)L.B;
+    a.A_f = (T *)L.Af;
+    a.B_f = (T *)L.Bf;
+    a.Y = (T *)L.Y;
+    a.C = (T *)L.C;
+    a.N = L.N;
+    a.Q = L.Q;
+    a.n = (int)h->n;
+    a.seq = L.seq ? 1 : 0;
+    a.level = l;
+    a.st = h->st;
+    return launch_chain_factor<Tin, T>(a, h->stream);
+}
+
+cudaError_t assemble_level(bss_handle *h, int l)
+{
+    Level &L = h->levels[l];
+    Level &X = h->levels[l + 1];
+    const int n = (int)h->n;
+    if (L.tin == F64 && L.t == F64)
+        return launch_assemble_schur<double, double, double>((const double *)L.A, (const double *)L.C,
+                                                             (double *)X.A, (double *)X.B, L.N, L.Q, n, h->stream);
+    if (L.tin == F32 && L.t == F32 && X.t == F32)
+        return launch_assemble_schur<float, float, float>((const float *)L.A, (const float *)L.C, (float *)X.A,
+                                                          (float *)X.B, L.N, L.Q, n, h->stream);
+    if (L.tin == F32 && L.t == F32 && X.t == F64)
+        return launch_assemble_schur<float, float, double>((const float *)L.A, (const float *)L.C, (double *)X.A,
+                                                           (double *)X.B, L.N, L.Q, n, h->stream);
+    if (L.tin == F64 && L.t == F32 && X.t == F32)
+        return launch_assemble_schur<double, float, float>((const double *)L.A, (const float *)L.C, (float *)X.A,
+                                                           (float *)X.B, L.N, L.Q, n, h->stream);
+    if (L.tin == F64 && L.t == F32 && X.t == F64)
+        return launch_assemble_schur<double, float, double>((const double *)L.A, (const float *)L.C,
+                                                            (double *)X.A, (double *)X.B, L.N, L.Q, n, h->stream);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t factor_any(bss_handle *h, int l)
+{
+    const Level &L = h->levels[l];
+    if (L.tin == F64 && L.t == F64) return factor_level<double, double>(h, l);
+    if (L.tin == F64 && L.t == F32) return factor_level<double, float>(h, l);
+    if (L.tin == F32 && L.t == F32) return factor_level<float, float>(h, l);
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+static int factorize_upto(bss_handle *h, int upto)
+{
+    BSS_CUDA(cudaMemsetAsync(&h->st->bad_key, 0xFF, sizeof(unsigned long long), h->stream));
+    const bool mixed = h->opt.precision == BSS_PRECISION_MIXED;
+    if (mixed) {
+        BSS_CUDA(cudaMemsetAsync(&h->st->anorm, 0, sizeof(unsigned long long), h->stream));
+        BSS_CUDA(launch_opnorm<double>((const double *)h->A, (const double *)h->B, h->N, (int)h->n, h->st,
+                                       h->stream));
+    }
+    const int nlev = (int)h->levels.size();
+    for (int l = 0; l < nlev && l < upto; ++l) {
+        BSS_CUDA(factor_any(h, l));
+        if (!h->levels[l].seq) BSS_CUDA(assemble_level(h, l));
+    }
+    h->factored = upto >= nlev;
+    h->sticky = BSS_OK;
+    return BSS_OK;
+}
+
+extern "C" int bss_factorize(bss_handle *h)
+{
+    if (!h) return fail(BSS_ERR_ARG, "handle is NULL");
+    return factorize_upto(h, (int)h->levels.size());
+}
+
+extern "C" int bss_factorize_levels(bss_handle *h, int32_t nlevels)
+{
+    if (!h) return fail(BSS_ERR_ARG, "handle is NULL");
+    if (nlevels < 0 || nlevels >= (int)h->levels.size())
+        return fail(BSS_ERR_ARG, "nlevels must be in [0, number of partitioned levels]");
+    return factorize_upto(h, nlevels);
+}
+
+extern "C" int bss_get_level(bss_handle *h, int32_t level, int64_t *N, int64_t *Q, void **A, void **B, void **d,
+                             int32_t *dtype)
+{
+    if (!h) return fail(BSS_ERR_ARG, "handle is NULL");
+    if (level < 0 || level >= (int)h->levels.size()) return fail(BSS_ERR_ARG, "level out of range");
+    const Level &L = h->levels[level];
+    if (N) *N = L.N;
+    if (Q) *Q = L.Q;
+    if (A) *A = L.A;
+    if (B) *B = L.B;
+    if (d) *d = L.d;
+    if (dtype) *dtype = L.t == F64 ? BSS_F64 : BSS_F32;
+    return BSS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// solve
+// ---------------------------------------------------------------------------
+namespace {
+
+template <class T>
+SolveArgs<T> solve_args(bss_handle *h, int l, int j0, int kc)
+{
+    Level &L = h->levels[l];
+    SolveArgs<T> a;
+    a.Af = (const T *)L.Af;
+    a.Bf = (const T *)L.Bf;
+    a.Y = (const T *)L.Y;
+    a.d = (T *)L.d;
+    a.bvec = (T *)L.bvec;
+    a.xsep = (l + 1 < (int)h->levels.size()) ? h->levels[l + 1].d : nullptr;
+    a.N = L.N;
+    a.Q = L.Q;
+    a.n = (int)h->n;
+    a.k = (int)h->k;
+    a.j0 = j0;
+    a.kc = kc;
+    a.seq = L.seq ? 1 : 0;
+    return a;
+}
+
+cudaError_t fwd_level(bss_handle *h, int l, int j0, int kc)
+{
+    const Level &L = h->levels[l];
+    if (L.t == F64) return launch_chain_fwd<double>(solve_args<double>(h, l, j0, kc), h->stream);
+    return launch_chain_fwd<float>(solve_args<float>(h, l, j0, kc), h->stream);
+}
+
+cudaError_t rhs_level(bss_handle *h, int l, int j0, int kc)
+{
+    const Level &L = h->levels[l];
+    const Level &X = h->levels[l + 1];
+    const int n = (int)h->n, k = (int)h->k;
+    if (L.t == F64 && X.t == F64)
+        return launch_assemble_rhs<double, double>((const double *)L.d, (const double *)L.bvec, (double *)X.d, L.N,
+                                                   L.Q, n, k, j0, kc, h->stream);
+    if (L.t == F32 && X.t == F32)
+        return launch_assemble_rhs<float, float>((const float *)L.d, (const float *)L.bvec, (float *)X.d, L.N, L.Q,
+                                                 n, k, j0, kc, h->stream);
+    if (L.t == F32 && X.t == F64)
+        return launch_assemble_rhs<float, double>((const float *)L.d, (const float *)L.bvec, (double *)X.d, L.N,
+                                                  L.Q, n, k, j0, kc, h->stream);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t bwd_level(bss_handle *h, int l, int j0, int kc)
+{
+    const Level &L = h->levels[l];
+    const Level &X = h->levels[l + 1];
+    if (L.t == F64 && X.t == F64) return launch_chain_bwd<double, double>(solve_args<double>(h, l, j0, kc), h->stream);
+    if (L.t == F32 && X.t == F32) return launch_chain_bwd<float, float>(solve_args<float>(h, l, j0, kc), h->stream);
+    if (L.t == F32 && X.t == F64) return launch_chain_bwd<float, double>(solve_args<float>(h, l, j0, kc), h->stream);
+    return cudaErrorInvalidValue;
+}
+
+// solve on levels[0].d in place, all k columns
+int chain_solve(bss_handle *h)
+{
+    const int nlev = (int)h->levels.size();
+    for (int j0 = 0; j0 < h->k; j0 += h->kc_max) {
+        const int kc = (int)std::min<long long>(h->kc_max, h->k - j0);
+        for (int l = 0; l + 1 < nlev; ++l) {
+            BSS_CUDA(fwd_level(h, l, j0, kc));
+            BSS_CUDA(rhs_level(h, l, j0, kc));
+        }
+        BSS_CUDA(fwd_level(h, nlev - 1, j0, kc));  // sequential coarsest: fwd + bwd
+        for (int l = nlev - 2; l >= 0; --l) BSS_CUDA(bwd_level(h, l, j0, kc));
+    }
+    return BSS_OK;
+}
+
+int solve_mixed(bss_handle *h)
+{
+    const long long cnt = h->N * h->n * h->k;
+    const double *d64 = (const double *)h->d;
+    const bool c_is_f32 = h->levels[0].t == F32;
+    DevStatus *st = h->st;
+    BSS_CUDA(cudaMemsetAsync(&st->dnorm, 0, sizeof(unsigned long long), h->stream));
+    BSS_CUDA(launch_absmax<double>(d64, cnt, &st->dnorm, h->stream));
+    if (c_is_f32)
+        BSS_CUDA((launch_convert<double, float>((float *)h->c0, d64, cnt, h->stream)));
+    else
+        BSS_CUDA((launch_convert<double, double>((double *)h->c0, d64, cnt, h->stream)));
+    int rc = chain_solve(h);
+    if (rc) return rc;
+    if (c_is_f32)
+        BSS_CUDA(launch_update<float>(h->x64, (const float *)h->c0, cnt, 1, h->stream));
+    else
+        BSS_CUDA(launch_update<double>(h->x64, (const double *)h->c0, cnt, 1, h->stream));
+    int steps = 0;
+    bool converged = false;
+    for (int it = 0; it <= h->opt.max_refine; ++it) {
+        BSS_CUDA(cudaMemsetAsync(&st->rnorm, 0, 2 * sizeof(unsigned long long), h->stream));
+        if (c_is_f32)
+            BSS_CUDA((launch_residual<double, float>((const double *)h->A, (const double *)h->B, h->x64, d64,
+                                                     (float *)h->c0, h->N, (int)h->n, (int)h->k, st, h->stream)));
+        else
+            BSS_CUDA((launch_residual<double, double>((const double *)h->A, (const double *)h->B, h->x64, d64,
+                                                      (double *)h->c0, h->N, (int)h->n, (int)h->k, st, h->stream)));
+        BSS_CUDA(launch_relres(st, h->opt.tol, h->stream));
+        BSS_CUDA(cudaMemcpyAsync(h->h_st, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->stream));
+        BSS_CUDA(cudaStreamSynchronize(h->stream));
+        h->info.rel_residual = h->h_st->relres;
+        if (h->h_st->done) {
+            converged = true;
+            break;
+        }
+        if (it == h->opt.max_refine) break;
+        rc = chain_solve(h);
+        if (rc) return rc;
+        if (c_is_f32)
+            BSS_CUDA(launch_update<float>(h->x64, (const float *)h->c0, cnt, 0, h->stream));
+        else
+            BSS_CUDA(launch_update<double>(h->x64, (const double *)h->c0, cnt, 0, h->stream));
+        ++steps;
+    }
+    h->info.refine_steps = steps;
+    BSS_CUDA(cudaMemcpyAsync(h->d, h->x64, cnt * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    if (!converged) h->sticky = BSS_ERR_NOT_CONVERGED;
+    return BSS_OK;
+}
+
+}  // namespace
+
+extern "C" int bss_solve(bss_handle *h)
+{
+    if (!h) return fail(BSS_ERR_ARG, "handle is NULL");
+    if (!h->factored) return fail(BSS_ERR_STATE, "solve before factorize");
+    if (h->opt.precision == BSS_PRECISION_MIXED) return solve_mixed(h);
+    return chain_solve(h);
+}
+
+extern "C" int bss_synchronize(bss_handle *h)
+{
+    if (!h) return fail(BSS_ERR_ARG, "handle is NULL");
+    BSS_CUDA(cudaStreamSynchronize(h->stream));
+    BSS_CUDA(cudaMemcpy(h->h_st, h->st, sizeof(DevStatus), cudaMemcpyDeviceToHost));
+    const unsigned long long key = h->h_st->bad_key;
+    if (h->factored && key != ~0ULL) {
+        h->info.failed_level = (int32_t)(key >> 40);
+        h->info.failed_block = (int64_t)(key & ((1ULL << 40) - 1));
+        return fail(BSS_ERR_NOT_SPD, "pivot failed at level " + std::to_string(h->info.failed_level) + ", block " +
+                                         std::to_string(h->info.failed_block));
+    }
+    h->info.failed_block = -1;
+    h->info.failed_level = -1;
+    if (h->sticky != BSS_OK) return fail(h->sticky, "refinement did not reach the tolerance");
+    return BSS_OK;
+}
+
+extern "C" int bss_get_info(bss_handle *h, bss_info *info)
+{
+    if (!h || !info) return fail(BSS_ERR_ARG, "NULL argument");
+    *info = h->info;
+    return BSS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// standalone residual
+// ---------------------------------------------------------------------------
+extern "C" int bss_residual(int64_t N, int64_t n, int64_t k, int32_t dtype, const void *A, const void *B,
+                            const void *x, const void *d, void *stream, double *out)
+{
+    if (!out || !A || !x || !d || N < 1 || n < 1 || k < 1) return fail(BSS_ERR_ARG, "bss_residual: bad argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    DevStatus *st = nullptr;
+    BSS_CUDA(cudaMallocAsync((void **)&st, sizeof(DevStatus), s));
+    BSS_CUDA(cudaMemsetAsync(st, 0, sizeof(DevStatus), s));
+    const long long cnt = N * n * k;
+    cudaError_t e;
+    if (dtype == BSS_F64) {
+        e = launch_opnorm<double>((const double *)A, (const double *)B, N, (int)n, st, s);
+        if (e == cudaSuccess) e = launch_absmax<double>((const double *)d, cnt, &st->dnorm, s);
+        if (e == cudaSuccess)
+            e = launch_residual<double, double>((const double *)A, (const double *)B, (const double *)x,
+                                                (const double *)d, nullptr, N, (int)n, (int)k, st, s);
+    } else {
+        e = launch_opnorm<float>((const float *)A, (const float *)B, N, (int)n, st, s);
+        if (e == cudaSuccess) e = launch_absmax<float>((const float *)d, cnt, &st->dnorm, s);
+        if (e == cudaSuccess)
+            e = launch_residual<float, float>((const float *)A, (const float *)B, (const float *)x, (const float *)d,
+                                              nullptr, N, (int)n, (int)k, st, s);
+    }
+    if (e == cudaSuccess) e = launch_relres(st, 0.0, s);
+    DevStatus hs;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(st, s);
+    if (e != cudaSuccess) return cuda_fail(e, "bss_residual");
+    *out = hs.relres;
+    return BSS_OK;
+}

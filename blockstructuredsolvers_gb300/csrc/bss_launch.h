@@ -1,0 +1,50 @@
+// Internal launcher interface between the C-ABI host code (bss_api.cu) and
+// the kernel translation units (k_*.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "bss_kernels.cuh"
+
+namespace bss {
+
+// largest block size the fused chain kernel handles in one CTA
+constexpr int MAX_FUSED_N = 64;
+
+int tile_for(int n);  // NB in {16, 32, 64}, or 0 if unsupported
+
+template <class Tin, class T>
+cudaError_t launch_chain_factor(const ChainFactorArgs<Tin, T> &a, cudaStream_t s);
+template <class Tin, class T>
+int chain_factor_ctas_per_sm(int n);
+
+template <class Tsrc, class T, class Tdst>
+cudaError_t launch_assemble_schur(const Tsrc *A_src, const T *C, Tdst *A_next, Tdst *B_next, long long N,
+                                  long long Q, int n, cudaStream_t s);
+
+template <class T>
+cudaError_t launch_chain_fwd(const SolveArgs<T> &a, cudaStream_t s);
+template <class T, class Tsep>
+cudaError_t launch_chain_bwd(const SolveArgs<T> &a, cudaStream_t s);
+template <class T, class Tn>
+cudaError_t launch_assemble_rhs(const T *d, const T *bvec, Tn *dn, long long N, long long Q, int n, int k, int j0,
+                                int kc, cudaStream_t s);
+
+template <class T>
+cudaError_t launch_opnorm(const T *A, const T *B, long long N, int n, DevStatus *st, cudaStream_t s);
+template <class T>
+cudaError_t launch_absmax(const T *v, long long count, unsigned long long *dst, cudaStream_t s);
+template <class T, class Tr>
+cudaError_t launch_residual(const T *A, const T *B, const T *x, const T *d, Tr *r, long long N, int n, int k,
+                            DevStatus *st, cudaStream_t s);
+cudaError_t launch_relres(DevStatus *st, double tol, cudaStream_t s);
+template <class Tc>
+cudaError_t launch_update(double *x, const Tc *c, long long count, int assign, cudaStream_t s);
+template <class Ts, class Td>
+cudaError_t launch_convert(Td *dst, const Ts *src, long long count, cudaStream_t s);
+template <class T>
+cudaError_t launch_init_identity(T *A, long long first_blk, long long last_blk, int n, cudaStream_t s);
+
+int solve_kc_max(int n, int k, int elem_bytes);
+
+}  // namespace bss

@@ -1,0 +1,158 @@
+// Launcher definitions, included by the per-dtype kernel translation units.
+#pragma once
+
+#include "bss_launch.h"
+
+namespace bss {
+
+inline int grid_for(long long work, int threads, int cap = 152 * 16)
+{
+    long long g = (work + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (int)g;
+}
+
+template <class Tin, class T, int NB>
+static cudaError_t chain_factor_nb(const ChainFactorArgs<Tin, T> &a, cudaStream_t s)
+{
+    const size_t smem = chain_factor_smem<T, NB>();
+    auto kern = chain_factor_kernel<Tin, T, NB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = a.seq ? 1u : (unsigned)a.Q;
+    kern<<<grid, Tile<NB>::THREADS, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class Tin, class T>
+cudaError_t launch_chain_factor(const ChainFactorArgs<Tin, T> &a, cudaStream_t s)
+{
+    switch (tile_for(a.n)) {
+    case 16: return chain_factor_nb<Tin, T, 16>(a, s);
+    case 32: return chain_factor_nb<Tin, T, 32>(a, s);
+    case 64: return chain_factor_nb<Tin, T, 64>(a, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <class Tin, class T, int NB>
+static int ctas_nb()
+{
+    const size_t smem = chain_factor_smem<T, NB>();
+    auto kern = chain_factor_kernel<Tin, T, NB>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
+    int nblk = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, kern, Tile<NB>::THREADS, smem) != cudaSuccess) return 1;
+    return nblk > 0 ? nblk : 1;
+}
+
+template <class Tin, class T>
+int chain_factor_ctas_per_sm(int n)
+{
+    switch (tile_for(n)) {
+    case 16: return ctas_nb<Tin, T, 16>();
+    case 32: return ctas_nb<Tin, T, 32>();
+    case 64: return ctas_nb<Tin, T, 64>();
+    default: return 1;
+    }
+}
+
+template <class Tsrc, class T, class Tdst>
+cudaError_t launch_assemble_schur(const Tsrc *A_src, const T *C, Tdst *A_next, Tdst *B_next, long long N,
+                                  long long Q, int n, cudaStream_t s)
+{
+    const long long work = (2 * Q + 1) * (long long)n * n;
+    assemble_schur_kernel<Tsrc, T, Tdst><<<grid_for(work, 256), 256, 0, s>>>(A_src, C, A_next, B_next, N, Q, n);
+    return cudaGetLastError();
+}
+
+template <class T>
+static cudaError_t set_solve_smem(const void *kern, size_t smem)
+{
+    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+template <class T>
+cudaError_t launch_chain_fwd(const SolveArgs<T> &a, cudaStream_t s)
+{
+    const size_t smem = solve_smem_bytes<T>(a.n, a.kc);
+    auto kern = chain_fwd_kernel<T>;
+    cudaError_t e = set_solve_smem<T>((const void *)kern, smem);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = a.seq ? 1u : (unsigned)a.Q;
+    kern<<<grid, SOLVE_THREADS, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class T, class Tsep>
+cudaError_t launch_chain_bwd(const SolveArgs<T> &a, cudaStream_t s)
+{
+    const size_t smem = solve_smem_bytes<T>(a.n, a.kc);
+    auto kern = chain_bwd_kernel<T, Tsep>;
+    cudaError_t e = set_solve_smem<T>((const void *)kern, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<(unsigned)a.Q, SOLVE_THREADS, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class T, class Tn>
+cudaError_t launch_assemble_rhs(const T *d, const T *bvec, Tn *dn, long long N, long long Q, int n, int k, int j0,
+                                int kc, cudaStream_t s)
+{
+    const long long work = (Q + 1) * (long long)n * kc;
+    assemble_rhs_kernel<T, Tn><<<grid_for(work, 256), 256, 0, s>>>(d, bvec, dn, N, Q, n, k, j0, kc);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_opnorm(const T *A, const T *B, long long N, int n, DevStatus *st, cudaStream_t s)
+{
+    opnorm_kernel<T><<<grid_for(N * n, 256), 256, 0, s>>>(A, B, N, n, st);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_absmax(const T *v, long long count, unsigned long long *dst, cudaStream_t s)
+{
+    absmax_kernel<T><<<grid_for(count, 256), 256, 0, s>>>(v, count, dst);
+    return cudaGetLastError();
+}
+
+template <class T, class Tr>
+cudaError_t launch_residual(const T *A, const T *B, const T *x, const T *d, Tr *r, long long N, int n, int k,
+                            DevStatus *st, cudaStream_t s)
+{
+    const size_t smem = (size_t)(n * (n + 1) + 3 * n * k) * sizeof(double);
+    auto kern = residual_kernel<T, Tr>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int threads = n * k < 256 ? ((n * k + 31) / 32) * 32 : 256;
+    kern<<<(unsigned)N, threads, smem, s>>>(A, B, x, d, r, N, n, k, st);
+    return cudaGetLastError();
+}
+
+template <class Tc>
+cudaError_t launch_update(double *x, const Tc *c, long long count, int assign, cudaStream_t s)
+{
+    update_kernel<Tc><<<grid_for(count, 256), 256, 0, s>>>(x, c, count, assign);
+    return cudaGetLastError();
+}
+
+template <class Ts, class Td>
+cudaError_t launch_convert(Td *dst, const Ts *src, long long count, cudaStream_t s)
+{
+    convert_kernel<Ts, Td><<<grid_for(count, 256), 256, 0, s>>>(dst, src, count);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_init_identity(T *A, long long first_blk, long long last_blk, int n, cudaStream_t s)
+{
+    if (last_blk <= first_blk) return cudaSuccess;
+    init_identity_kernel<T><<<grid_for((last_blk - first_blk) * (long long)n * n, 256), 256, 0, s>>>(
+        A, first_blk, last_blk, n);
+    return cudaGetLastError();
+}
+
+}  // namespace bss
