@@ -1,0 +1,439 @@
+"""Benchmark: factorize! + solve! of one block-tridiagonal SPD system,
+N = 16384 blocks of n = 64, k = 1 right-hand side (BASELINE config 1:
+A_i = G G^T + n I, B_i ~ N(0,1), d ~ U[0,1), seeded, generated on the GPU).
+
+A "step" is one complete solve request: put d into the handle, factorize!,
+solve!, to a relative residual ||d - A x||_inf / (||A|| ||x|| + ||d||)
+<= 1e-12.  The headline path is the mixed-precision one (FP32 chain
+factorization on the sm_103a kernels + FP64 iterative refinement); the same
+JSON line carries the plain FP64 and plain FP32 GPU paths for comparison.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference's CPU path (cpu.jl / backbone_cpu.jl
+restated in C on OpenBLAS, ``oracle/``) on the host cores instead.
+Multi-GPU: the solver does not shard a single system across GPUs here, so
+each rank runs an independent replica ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_BLK, N_SZ, K_RHS = 16384, 64, 1
+METRIC = "solves/s (factorize!+solve!, rel-resid <= 1e-12)"
+WORKLOAD = "block-tridiagonal SPD, N=16384 blocks of n=64, k=1 (A_i=G G^T+nI, B_i~N(0,1), d~U[0,1))"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="skip the secondary legs")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# --------------------------------------------------------------------------
+# CPU reference arm / baseline (oracle: test infrastructure, timed only here)
+# --------------------------------------------------------------------------
+def gen_host(seed=1):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    G = rng.standard_normal((N_BLK, N_SZ, N_SZ))
+    A = G @ np.swapaxes(G, 1, 2) + N_SZ * np.eye(N_SZ)
+    B = rng.standard_normal((N_BLK - 1, N_SZ, N_SZ))
+    d = rng.random((N_BLK, N_SZ, K_RHS))
+    # Julia column-major storage: (N, c, r) C-order
+    return (np.ascontiguousarray(np.swapaxes(A, 1, 2)), np.ascontiguousarray(np.swapaxes(B, 1, 2)),
+            np.ascontiguousarray(np.swapaxes(d, 1, 2)))
+
+
+def cpu_solve_time(As, Bs, ds, reps=1, threads=None):
+    """Seconds per factorize!+solve! of the reference CPU path (C restatement
+    of backbone_cpu.jl on OpenBLAS) on copies of the inputs."""
+    from oracle import cref
+    cref.lib(True)
+    if threads is not None:
+        cref.set_blas_threads(threads)
+    ts = []
+    for _ in range(reps):
+        A, B, d = As.copy(), Bs.copy(), ds.copy()
+        t0 = time.perf_counter()
+        info = cref.solve(A, B, d)
+        ts.append(time.perf_counter() - t0)
+        assert info == 0
+    return min(ts), d
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    As, Bs, ds = gen_host()
+    cores = os.cpu_count() or 1
+    # the reference CPU path is a sequential block chain; BLAS threads are the
+    # only host parallelism it has.  Use whichever thread count is faster.
+    best = None
+    for th in sorted({1, cores}):
+        t, _ = cpu_solve_time(As, Bs, ds, reps=1, threads=th)
+        if best is None or t < best[0]:
+            best = (t, th)
+    th = best[1]
+    from oracle import cref
+    cref.set_blas_threads(th)
+    for _ in range(max(args.warmup, 0)):
+        cpu_solve_time(As, Bs, ds, reps=1)
+    ts = []
+    for _ in range(args.steps):
+        t, _ = cpu_solve_time(As, Bs, ds, reps=1)
+        ts.append(t)
+    total = sum(ts)
+    val = args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy, config 1 generator)",
+        "config": {"workload": WORKLOAD, "N": N_BLK, "n": N_SZ, "k": K_RHS},
+        "cpu_baseline": {"value": val, "unit": "solves/s", "cores": th, "kind": "port",
+                         "sample": f"{args.steps} full factorize!+solve! of the workload, OpenBLAS "
+                                   f"({th} thread(s)) via the C restatement of backbone_cpu.jl"},
+        "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks + throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                                 f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def gen_device(dev, seed=1):
+    import torch
+    g = torch.Generator(device=dev).manual_seed(seed)
+    G = torch.randn(N_BLK, N_SZ, N_SZ, device=dev, dtype=torch.float64, generator=g)
+    A = G @ G.transpose(1, 2) + N_SZ * torch.eye(N_SZ, device=dev, dtype=torch.float64)
+    del G
+    B = torch.randn(N_BLK - 1, N_SZ, N_SZ, device=dev, dtype=torch.float64, generator=g)
+    d = torch.rand(N_BLK, N_SZ, K_RHS, device=dev, dtype=torch.float64, generator=g)
+    # column-major (n, n, N) views, as the handle tensors are laid out
+    return A.permute(1, 2, 0), B.permute(1, 2, 0), d.permute(1, 2, 0)
+
+
+def rel_residual_dev(A, B, x, d):
+    """FP64 relative residual with torch on the device (checker only)."""
+    import torch
+    Am, Bm, xm, dm = (t.permute(2, 0, 1) for t in (A, B, x, d))
+    r = dm - Am @ xm
+    r[:-1] -= Bm @ xm[1:]
+    r[1:] -= Bm.transpose(1, 2) @ xm[:-1]
+    rs = Am.abs().sum(2)
+    rs[:-1] += Bm.abs().sum(2)
+    rs[1:] += Bm.abs().sum(1)
+    return (r.abs().max() / (rs.max() * xm.abs().max() + dm.abs().max())).item()
+
+
+def time_leg(bss, A, B, d, T, precision, steps, warmup, restore_AB, ev_stream=None):
+    """K timed steps; returns (seconds total, factor ms list, solve ms list, data)."""
+    import torch
+    N = N_BLK
+    data = bss.initialize_batched(N, N_SZ, T, k=K_RHS, precision=precision)
+    At, Bt, dt = data.A_tensor[:, :, :N], data.B_tensor[:, :, :N - 1], data.d_tensor[:, :, :N]
+    Ac, Bc, dc = A.to(T), B.to(T), d.to(T)
+    At.copy_(Ac)
+    Bt.copy_(Bc)
+
+    def step(record=None):
+        if restore_AB:
+            At.copy_(Ac)
+            Bt.copy_(Bc)
+        dt.copy_(dc)
+        if record:
+            record[0].record()
+        bss.factorize_(data)
+        if record:
+            record[1].record()
+        bss.solve_(data)
+        if record:
+            record[2].record()
+
+    for _ in range(warmup):
+        step()
+    bss.synchronize(data)
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for s in range(steps):
+        step(evs[s])
+    t1.record()
+    bss.synchronize(data)
+    torch.cuda.synchronize()
+    total_ms = t0.elapsed_time(t1)
+    fac = [e[0].elapsed_time(e[1]) for e in evs]
+    sol = [e[1].elapsed_time(e[2]) for e in evs]
+    return total_ms / 1e3, fac, sol, data
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import blockstructuredsolvers_gb300 as bss
+    from blockstructuredsolvers_gb300 import _lib
+    L = _lib.load()
+
+    A, B, d = gen_device(dev)
+    # ---- headline: mixed precision, inputs resident in HBM -------------------
+    sampler = ClockSampler(local)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = L.bss_kernel_launches()
+    sampler.start()
+    secs, fac, sol, data = time_leg(bss, A, B, d, torch.float64, "mixed", args.steps, args.warmup, False)
+    clocks = sampler.stop()
+    launches = L.bss_kernel_launches() - launches0
+    info = bss.get_info(data)
+    x = data.d_tensor[:, :, :N_BLK]
+    relres = rel_residual_dev(A, B, x, d)
+    launches_per_step = None
+    # the warmup steps launched too: count per step from the total
+    launches_per_step = launches / max(args.steps + args.warmup, 1)
+    if world > 1:
+        t = torch.tensor([secs], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        secs = t.item()
+    value = world * args.steps / secs
+
+    extra = {}
+    if not args.quick:
+        # ---- plain FP64 and plain FP32 GPU paths (same request) ---------------
+        s64, f64, so64, d64 = time_leg(bss, A, B, d, torch.float64, "plain", max(3, args.steps // 4), 1, True)
+        rr64 = rel_residual_dev(A, B, d64.d_tensor[:, :, :N_BLK], d)
+        del d64
+        s32, f32, so32, d32 = time_leg(bss, A, B, d, torch.float32, "plain", max(3, args.steps // 4), 1, True)
+        rr32 = rel_residual_dev(A.float().double(), B.float().double(), d32.d_tensor[:, :, :N_BLK].double(),
+                                d.float().double())
+        del d32
+        n64 = max(3, args.steps // 4)
+        extra["plain_fp64"] = {"solves_per_s": n64 / s64, "factor_ms": statistics.median(f64),
+                               "solve_ms": statistics.median(so64), "rel_residual": rr64,
+                               "note": "includes the device copy of A, B, d into the handle per step"}
+        extra["plain_fp32"] = {"solves_per_s": n64 / s32, "factor_ms": statistics.median(f32),
+                               "solve_ms": statistics.median(so32), "rel_residual_fp32_system": rr32,
+                               "note": "FP32 accuracy only; not a rel-resid <= 1e-12 result"}
+
+    # ---- e2e through the public API with host buffers ----------------------
+    e2e = None
+    if not args.quick:
+        Ah = A.permute(2, 0, 1).contiguous().cpu().pin_memory()  # (N, c, r) storage == column-major blocks
+        Bh = B.permute(2, 0, 1).contiguous().cpu().pin_memory()
+        dh = d.permute(2, 0, 1).contiguous().cpu().pin_memory()
+        xh = torch.empty_like(dh).pin_memory()
+        data = bss.initialize_batched(N_BLK, N_SZ, torch.float64, k=K_RHS, precision="mixed")
+        At = data.A_tensor[:, :, :N_BLK].permute(2, 1, 0)  # (N, c, r) view of column-major storage
+        Bt = data.B_tensor[:, :, :N_BLK - 1].permute(2, 1, 0)
+        dt = data.d_tensor[:, :, :N_BLK].permute(2, 1, 0)
+        ne = max(3, args.steps // 4)
+
+        def e2e_step():
+            At.copy_(Ah.permute(0, 2, 1).transpose(1, 2), non_blocking=True)
+            Bt.copy_(Bh.permute(0, 2, 1).transpose(1, 2), non_blocking=True)
+            dt.copy_(dh.permute(0, 2, 1).transpose(1, 2), non_blocking=True)
+            bss.factorize_(data)
+            bss.solve_(data)
+            xh.copy_(dt, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        tt0 = time.perf_counter()
+        for _ in range(ne):
+            e2e_step()
+        torch.cuda.synchronize()
+        te = time.perf_counter() - tt0
+        bi = (Ah.numel() + Bh.numel() + dh.numel()) * 8
+        bo = xh.numel() * 8
+        e2e = {"value": world * ne / te, "unit": "solves/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo}
+        xs = xh.permute(0, 2, 1).numpy()  # math (N, n, k)
+        del data
+
+    # ---- roofline of the dominant kernel ----------------------------------
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs")
+    peak_kind = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    roof = roofline_chain_factor(bss, A, B, d, hbm, peak_kind)
+
+    cpu_base = None
+    if rank == 0 and not args.no_cpu_baseline and world == 1:
+        try:
+            As = A.permute(2, 1, 0).contiguous().cpu().numpy()
+            Bs = B.permute(2, 1, 0).contiguous().cpu().numpy()
+            ds = d.permute(2, 1, 0).contiguous().cpu().numpy()
+            from oracle import cref
+            cores = os.cpu_count() or 1
+            t1, _ = cpu_solve_time(As, Bs, ds, reps=1, threads=1)
+            tN, xcpu = cpu_solve_time(As, Bs, ds, reps=1, threads=cores)
+            best = min((t1, 1), (tN, cores))
+            cpu_base = {"value": 1.0 / best[0], "unit": "solves/s", "cores": best[1], "kind": "port",
+                        "sample": "one full factorize!+solve! of the workload (C restatement of "
+                                  "backbone_cpu.jl on OpenBLAS); best of 1 thread and "
+                                  f"{cores} BLAS threads"}
+        except Exception as e:  # pragma: no cover
+            cpu_base = {"value": None, "unit": "solves/s", "cores": None, "kind": "port", "sample": f"failed: {e}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 factor + f64 refinement",
+            "data": "synthetic (seeded torch generator on device, config 1 distribution)",
+            "config": {"workload": WORKLOAD, "N": N_BLK, "n": N_SZ, "k": K_RHS, "precision": "mixed",
+                       "levels": info["levels"], "coarsest_blocks": info["coarsest_blocks"],
+                       "l2": "inputs (1.07 GB FP64 A,B) larger than L2; no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "factor_ms_median": statistics.median(fac), "solve_ms_median": statistics.median(sol),
+            "refine_steps": info["refine_steps"], "rel_residual": relres,
+            "gpu_launches": int(round(launches_per_step * args.steps)),
+            "gpu_launches_per_step": launches_per_step,
+            "clocks": clocks, "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e,
+        }
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def roofline_chain_factor(bss, A, B, d, hbm_gbs, peak_kind):
+    """Roofline of the dominant kernel of the mixed path: the level-0 chain
+    factor kernel (FP64 A_i, B_i in; FP32 V_i, W_i, Y_i out).  Algorithmic
+    bytes per launch = sum over interior blocks of 2 n^2 * 8 (A_i, B_i read)
+    + 3 n^2 * 4 (V, W, Y written); duration from CUDA events around a
+    factorize_levels(1) call (the level-0 chain kernel + its assembly)."""
+    import torch
+    from blockstructuredsolvers_gb300 import _lib
+    L = _lib.load()
+    data = bss.initialize_batched(N_BLK, N_SZ, torch.float64, k=K_RHS, precision="mixed")
+    data.A_tensor[:, :, :N_BLK].copy_(A)
+    data.B_tensor[:, :, :N_BLK - 1].copy_(B)
+    info = bss.get_info(data)
+    torch.cuda.synchronize()
+    ts = []
+    for r in range(6):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _lib.check(L.bss_factorize_levels(data.handle, 1))
+        e1.record()
+        torch.cuda.synchronize()
+        if r:
+            ts.append(e0.elapsed_time(e1))
+    import ctypes
+    Nl = ctypes.c_int64()
+    Q = ctypes.c_int64()
+    _lib.check(L.bss_get_level(data.handle, 0, ctypes.byref(Nl), ctypes.byref(Q), None, None, None, None))
+    interior = Nl.value - (Q.value + 1)
+    nn = N_SZ * N_SZ
+    alg_bytes = interior * (2 * nn * 8 + 3 * nn * 4) + (Q.value + 1) * nn * 8
+    ms = statistics.median(ts)
+    ach = alg_bytes / (ms * 1e-3) / 1e9
+    return {"kernel": "chain_factor_kernel<double,float,64> (level 0) + assemble_schur", "bound": "hbm",
+            "achieved": ach, "peak": hbm_gbs, "unit": "GB/s", "frac": ach / hbm_gbs,
+            "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})", "duration_ms": ms,
+            "algorithmic_bytes": alg_bytes, "partitions": Q.value, "traffic": None,
+            "note": "latency/FMA-bound chain: the HBM fraction is low by construction"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -34,7 +34,7 @@ EXPORTS = (
     "bss_default_options", "bss_create_batched", "bss_create_seq", "bss_destroy",
     "bss_get_tensors", "bss_get_dims", "bss_factorize", "bss_solve", "bss_synchronize",
     "bss_get_info", "bss_last_error_string", "bss_plan_reference", "bss_residual",
-    "bss_factorize_levels", "bss_get_level", "bss_version",
+    "bss_factorize_levels", "bss_get_level", "bss_kernel_launches", "bss_version",
 )
 
 
@@ -105,10 +105,12 @@ def load(path: str | None = None):
     L.bss_factorize_levels.argtypes = [vp, i32]
     L.bss_get_level.argtypes = [vp, i32, ctypes.POINTER(i64), ctypes.POINTER(i64), ctypes.POINTER(vp),
                                 ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(i32)]
+    L.bss_kernel_launches.argtypes = []
+    L.bss_kernel_launches.restype = ctypes.c_int64
     L.bss_version.argtypes = []
     L.bss_version.restype = ctypes.c_char_p
     for name in EXPORTS:
-        if name not in ("bss_default_options", "bss_last_error_string", "bss_version"):
+        if name not in ("bss_default_options", "bss_last_error_string", "bss_version", "bss_kernel_launches"):
             getattr(L, name).restype = ctypes.c_int
     if path is None:
         _lib = L

@@ -102,6 +102,8 @@ extern "C" void bss_default_options(bss_options *o)
 
 extern "C" const char *bss_last_error_string(void) { return g_last_error.c_str(); }
 
+extern "C" int64_t bss_kernel_launches(void) { return (int64_t)launch_count(); }
+
 extern "C" const char *bss_version(void)
 {
     return "bss-gb300 0.1 (sm_103a; fused chain kernels n<=64; FP32/FP64/mixed)";

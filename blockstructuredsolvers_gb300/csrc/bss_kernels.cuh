@@ -233,92 +233,188 @@ __device__ __forceinline__ T safe_pivot(T p)
     return (p > T(0) && p < T(INFINITY)) ? p : T(1);
 }
 
-// In-register Cholesky (lower, L L^T = S) fused with M = L^{-1}.
-// S holds the symmetric tile (identity outside n x n).  On return M holds
-// L^{-1} (lower triangular, identity outside n x n).  One __syncthreads per
-// column: column j of the trailing matrix and row j-1 of M are published
-// through small shared buffers (colbuf triple-, rowbuf double-buffered).
-// Returns true in the thread that owns (j,j) if pivot j failed.
-template <class T, int NB>
-__device__ __forceinline__ int chol_inv_regs(T (&S)[Tile<NB>::RA][Tile<NB>::RB], T (&M)[Tile<NB>::RA][Tile<NB>::RB],
-                                             T *colbuf, T *rowbuf, int n, int ti, int tj)
-{
-    using TL = Tile<NB>;
-    int bad = 0;
-#pragma unroll
-    for (int a = 0; a < TL::RA; ++a)
-#pragma unroll
-        for (int b = 0; b < TL::RB; ++b) M[a][b] = ((ti + TL::TI * a) == (tj + TL::TJ * b)) ? T(1) : T(0);
+// ---------------------------------------------------------------------------
+// Blocked upper Cholesky + inverse of an NB x NB SPD tile in shared memory.
+// On entry sS holds S; only its upper triangle is read (as LAPACK potrf 'U'
+// in the reference's backbone_cpu.jl:7,13 / cusolverDnXpotrf(Batched) 'U').
+// On exit sS's upper triangle holds U (U^T U = S), its lower triangle is
+// scratch, and sV holds V = U^{-1} (upper, zeros below the diagonal -- the
+// caller zeroes sV's strictly lower 16x16 tiles once).
+// Panels are PB = 16 wide: one warp factors each 16x16 diagonal tile with
+// shuffles (lane r owns column r), another warp inverts it by per-lane back
+// substitution while the rest of the CTA solves the row panel; the trailing
+// matrix update and the NB/16-1 block stages of V are spread over the CTA.
+// ---------------------------------------------------------------------------
+constexpr int PB = 16;
 
-    for (int j = 0; j <= n; ++j) {
-        // publish column j of the trailing matrix (final after step j-1)
-        if (j < n && tj == (j % TL::TJ)) {
-            const int bj = j / TL::TJ;
+template <class T, int LD>
+__device__ __forceinline__ int warp_chol16(T *sS, T *dinv, int o, int lane)
+{
+    const int r = lane & (PB - 1);
+    T u[PB];
 #pragma unroll
-            for (int b = 0; b < TL::RB; ++b)
-                if (b == bj) {
+    for (int c = 0; c < PB; ++c) u[c] = sS[(o + c) + (o + r) * LD];  // S(o+c, o+r), valid for c <= r
+    int bad = 0;
+    T udiag = T(1);
 #pragma unroll
-                    for (int a = 0; a < TL::RA; ++a) {
-                        const int r = ti + TL::TI * a;
-                        if (r >= j) {
-                            colbuf[(j % 3) * NB + r] = S[a][b];
-                            if (r == j && !(S[a][b] > T(0) && S[a][b] < T(INFINITY))) bad = j + 1;
-                        }
-                    }
-                }
+    for (int j = 0; j < PB; ++j) {
+        T piv = __shfl_sync(0xffffffffu, u[j], j);
+        if (!(piv > T(0) && piv < T(INFINITY))) {
+            bad = 1;
+            piv = T(1);
         }
-        // publish row j-1 of M, scaled by 1/L(j-1,j-1)
-        if (j >= 1 && ti == ((j - 1) % TL::TI)) {
-            const int aj = (j - 1) / TL::TI;
-            const T linv = T(1) / sqrt(safe_pivot(colbuf[((j - 1) % 3) * NB + (j - 1)]));
+        const T ujr = u[j] * (T(1) / sqrt(piv));  // U(j, r), r >= j
+        u[j] = ujr;
+        if (j == r) udiag = ujr;
 #pragma unroll
-            for (int a = 0; a < TL::RA; ++a)
-                if (a == aj) {
-#pragma unroll
-                    for (int b = 0; b < TL::RB; ++b) {
-                        const T v = M[a][b] * linv;
-                        M[a][b] = v;
-                        rowbuf[((j - 1) & 1) * NB + tj + TL::TJ * b] = v;
-                    }
-                }
-        }
-        __syncthreads();
-        if (j < n) {
-            const T *col = colbuf + (j % 3) * NB;
-            const T pinv = T(1) / safe_pivot(col[j]);
-            T cr[TL::RA], cc[TL::RB];
-#pragma unroll
-            for (int a = 0; a < TL::RA; ++a) cr[a] = col[ti + TL::TI * a] * pinv;
-#pragma unroll
-            for (int b = 0; b < TL::RB; ++b) cc[b] = col[tj + TL::TJ * b];
-#pragma unroll
-            for (int a = 0; a < TL::RA; ++a)
-#pragma unroll
-                for (int b = 0; b < TL::RB; ++b) {
-                    const int r = ti + TL::TI * a, c = tj + TL::TJ * b;
-                    if (r > j && c > j && r < n && c < n) S[a][b] = fma(-cr[a], cc[b], S[a][b]);
-                }
-        }
-        if (j >= 1) {
-            const int jm = j - 1;
-            const T *col = colbuf + (jm % 3) * NB;
-            const T *row = rowbuf + (jm & 1) * NB;
-            const T linv = T(1) / sqrt(safe_pivot(col[jm]));
-            T rv[TL::RB];
-#pragma unroll
-            for (int b = 0; b < TL::RB; ++b) rv[b] = row[tj + TL::TJ * b];
-#pragma unroll
-            for (int a = 0; a < TL::RA; ++a) {
-                const int r = ti + TL::TI * a;
-                if (r > jm && r < n) {
-                    const T l = col[r] * linv;  // L(r, j-1)
-#pragma unroll
-                    for (int b = 0; b < TL::RB; ++b) M[a][b] = fma(-l, rv[b], M[a][b]);
-                }
-            }
+        for (int c = j + 1; c < PB; ++c) {
+            const T ujc = __shfl_sync(0xffffffffu, ujr, c);  // U(j, c) from lane c
+            u[c] = fma(-ujc, ujr, u[c]);                      // S(c, r) -= U(j,c) U(j,r)
         }
     }
+    if (lane < PB) {
+#pragma unroll
+        for (int c = 0; c < PB; ++c)
+            if (c <= r) sS[(o + c) + (o + r) * LD] = u[c];
+        dinv[o + r] = T(1) / udiag;
+    }
     return bad;
+}
+
+// V_KK = U_KK^{-1}: lane r computes column r by back substitution.
+template <class T, int LD>
+__device__ __forceinline__ void warp_inv16(const T *sS, const T *dinv, T *sV, int o, int lane)
+{
+    const int r = lane & (PB - 1);
+    T v[PB];
+#pragma unroll
+    for (int q = PB - 1; q >= 0; --q) {
+        T s0 = (q == r) ? T(1) : T(0), s1 = T(0);
+#pragma unroll
+        for (int t = q + 1; t < PB; ++t) {
+            if ((t & 1) == 0)
+                s0 = fma(-sS[(o + q) + (o + t) * LD], v[t], s0);
+            else
+                s1 = fma(-sS[(o + q) + (o + t) * LD], v[t], s1);
+        }
+        v[q] = (s0 + s1) * dinv[o + q];
+    }
+    if (lane < PB) {
+#pragma unroll
+        for (int c = 0; c < PB; ++c) sV[(o + c) + (o + r) * LD] = v[c];
+    }
+}
+
+// row panel right of diagonal tile o: U(o:o+16, c) = U_KK^{-T} S(o:o+16, c)
+template <class T, int LD, int NB>
+__device__ __forceinline__ void panel_trsm(T *sS, const T *dinv, int o, int t0, int nthr)
+{
+    for (int c = o + PB + t0; c < NB; c += nthr) {
+        T x[PB];
+#pragma unroll
+        for (int p = 0; p < PB; ++p) x[p] = sS[(o + p) + c * LD];
+#pragma unroll
+        for (int p = 0; p < PB; ++p) {
+            x[p] *= dinv[o + p];
+#pragma unroll
+            for (int q = p + 1; q < PB; ++q) x[q] = fma(-sS[(o + p) + (o + q) * LD], x[p], x[q]);
+        }
+#pragma unroll
+        for (int p = 0; p < PB; ++p) sS[(o + p) + c * LD] = x[p];
+    }
+}
+
+// S(a, b) -= sum_p U(o+p, a) U(o+p, b)   for o+16 <= a <= b < NB
+template <class T, int LD, int NB>
+__device__ __forceinline__ void trailing_update(T *sS, int o, int tid, int nthr)
+{
+    using V = typename Vec<T>::type;
+    constexpr int W = Vec<T>::W;
+    const int m = NB - o - PB;
+    for (int e = tid; e < m * m; e += nthr) {
+        const int b = e / m;
+        const int a = e - b * m;
+        if (a > b) continue;
+        const int ca = o + PB + a, cb = o + PB + b;
+        T acc = T(0);
+#pragma unroll
+        for (int p = 0; p < PB; p += W) {
+            const V x = *reinterpret_cast<const V *>(sS + (o + p) + ca * LD);
+            const V y = *reinterpret_cast<const V *>(sS + (o + p) + cb * LD);
+            fma_vec(acc, x, y);
+        }
+        sS[ca + cb * LD] -= acc;
+    }
+}
+
+// off-diagonal tiles of V = U^{-1}:  V_IJ = -V_II sum_{P=I+1..J} U_IP V_PJ,
+// one super-diagonal stage at a time (s = J - I).  T_IJ is kept in the
+// (scratch) lower tile (J, I) of sS.
+template <class T, int LD, int NB>
+__device__ __forceinline__ void inverse_stages(T *sS, T *sV, int tid, int nthr)
+{
+    constexpr int KP = NB / PB;
+#pragma unroll 1
+    for (int s = 1; s < KP; ++s) {
+        const int ntile = KP - s;
+        for (int e = tid; e < ntile * PB * PB; e += nthr) {
+            const int tile = e / (PB * PB), w = e - tile * PB * PB;
+            const int a = w % PB, b = w / PB;
+            const int I = tile, J = tile + s;
+            T acc = T(0);
+            for (int P = I + 1; P <= J; ++P)
+#pragma unroll
+                for (int q = 0; q < PB; ++q)
+                    acc = fma(sS[(PB * I + a) + (PB * P + q) * LD], sV[(PB * P + q) + (PB * J + b) * LD], acc);
+            sS[(PB * J + a) + (PB * I + b) * LD] = acc;
+        }
+        __syncthreads();
+        for (int e = tid; e < ntile * PB * PB; e += nthr) {
+            const int tile = e / (PB * PB), w = e - tile * PB * PB;
+            const int a = w % PB, b = w / PB;
+            const int I = tile, J = tile + s;
+            T acc = T(0);
+#pragma unroll
+            for (int c = 0; c < PB; ++c)
+                if (c >= a) acc = fma(sV[(PB * I + a) + (PB * I + c) * LD], sS[(PB * J + c) + (PB * I + b) * LD], acc);
+            sV[(PB * I + a) + (PB * J + b) * LD] = -acc;
+        }
+        __syncthreads();
+    }
+}
+
+// Factor the tile in sS into sV = U^{-1}.  Returns nonzero (in every thread)
+// if a pivot failed.  Ends with a __syncthreads.
+template <class T, int NB, int THREADS>
+__device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sflag, int tid)
+{
+    constexpr int LD = Geo<T, NB>::LD;
+    constexpr int KP = NB / PB;
+    const int warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) *sflag = 0;
+#pragma unroll 1
+    for (int K = 0; K < KP; ++K) {
+        const int o = PB * K;
+        if (warp == 0) {
+            const int bad = warp_chol16<T, LD>(sS, dinv, o, lane);
+            if (bad && lane == 0) *sflag = 1;
+        }
+        __syncthreads();
+        if (warp == (THREADS > 32 ? 1 : 0)) warp_inv16<T, LD>(sS, dinv, sV, o, lane);
+        if (K + 1 < KP) {
+            if (THREADS > 32) {
+                const int t0 = warp == 0 ? lane : tid - 32;
+                if (warp != 1) panel_trsm<T, LD, NB>(sS, dinv, o, t0, THREADS - 32);
+            } else {
+                panel_trsm<T, LD, NB>(sS, dinv, o, tid, THREADS);
+            }
+            __syncthreads();
+            trailing_update<T, LD, NB>(sS, o, tid, THREADS);
+        }
+        __syncthreads();
+    }
+    inverse_stages<T, LD, NB>(sS, sV, tid, THREADS);
+    return *sflag;
 }
 
 // ---------------------------------------------------------------------------
@@ -343,11 +439,11 @@ struct ChainFactorArgs {
 template <class T, int NB>
 constexpr size_t chain_factor_smem()
 {
-    return (size_t)(5 * Geo<T, NB>::SLOT + 5 * NB) * sizeof(T);
+    return (size_t)(6 * Geo<T, NB>::SLOT + NB) * sizeof(T) + 16;
 }
 
 template <class Tin, class T, int NB>
-__global__ void __launch_bounds__(Tile<NB>::THREADS) chain_factor_kernel(ChainFactorArgs<Tin, T> g)
+__global__ void __launch_bounds__(Tile<NB>::THREADS, sizeof(T) == 4 ? 2 : 1) chain_factor_kernel(ChainFactorArgs<Tin, T> g)
 {
     using TL = Tile<NB>;
     constexpr int LD = Geo<T, NB>::LD;
@@ -358,8 +454,9 @@ __global__ void __launch_bounds__(Tile<NB>::THREADS) chain_factor_kernel(ChainFa
     T *sY = sW + SLOT;
     T *sZ = sY + SLOT;
     T *sB = sZ + SLOT;
-    T *colbuf = sB + SLOT;   // 3*NB
-    T *rowbuf = colbuf + 3 * NB;  // 2*NB
+    T *sS = sB + SLOT;
+    T *dinv = sS + SLOT;                              // NB
+    int *sflag = reinterpret_cast<int *>(dinv + NB);
 
     const int tid = threadIdx.x;
     const int ti = tid % TL::TI, tj = tid / TL::TI;
@@ -381,6 +478,8 @@ __global__ void __launch_bounds__(Tile<NB>::THREADS) chain_factor_kernel(ChainFa
 
     T accLL[TL::RA][TL::RB];
     zero_tile<T, NB>(accLL);
+    for (int e = tid; e < SLOT; e += TL::THREADS) sV[e] = T(0);  // V's strictly lower tiles stay zero
+    __syncthreads();
 
     for (long long i = first; i <= last; ++i) {
         const long long t = i - first;
@@ -410,20 +509,11 @@ __global__ void __launch_bounds__(Tile<NB>::THREADS) chain_factor_kernel(ChainFa
         T Bi[TL::RA][TL::RB];
         if (has_next) load_tile<Tin, T, NB>(Bi, g.B_in + i * nn, n, ti, tj, false, false);
 
-        T M[TL::RA][TL::RB];
-        const int bad = chol_inv_regs<T, NB>(S, M, colbuf, rowbuf, n, ti, tj);
-        if (bad) record_bad_pivot(g.st, g.level, i);
-
-        // V = M^T into sV (V(k, i) at k + i*LD; M(r,c) = V(c,r)); B_i into sB
-#pragma unroll
-        for (int a = 0; a < TL::RA; ++a)
-#pragma unroll
-            for (int b = 0; b < TL::RB; ++b) {
-                const int r = ti + TL::TI * a, c = tj + TL::TJ * b;
-                sV[c + r * LD] = M[a][b];
-                if (has_next) sB[r + c * LD] = Bi[a][b];
-            }
+        store_tile_smem<T, NB>(sS, S, ti, tj, T(1));
+        if (has_next) store_tile_smem<T, NB>(sB, Bi, ti, tj, T(1));
         __syncthreads();
+        const int bad = chol_inv_blocked<T, NB, TL::THREADS>(sS, sV, dinv, sflag, tid);
+        if (bad && tid == 0) record_bad_pivot(g.st, g.level, i);
 
         T accY[TL::RA][TL::RB], accW[TL::RA][TL::RB];
         zero_tile<T, NB>(accY);
@@ -436,8 +526,9 @@ __global__ void __launch_bounds__(Tile<NB>::THREADS) chain_factor_kernel(ChainFa
         // V -> global (coalesced copy from sV)
         {
             T *dst = g.A_f + i * nn;
-            for (long long e = tid; e < nn; e += TL::THREADS) {
-                const int r = (int)(e % n), c = (int)(e / n);
+            const int nn32 = n * n;
+            for (int e = tid; e < nn32; e += TL::THREADS) {
+                const int c = e / n, r = e - c * n;
                 dst[e] = sV[r + c * LD];
             }
         }
@@ -496,17 +587,51 @@ __global__ void assemble_schur_kernel(const Tsrc *__restrict__ A_src, const T *_
 }
 
 // ---------------------------------------------------------------------------
-// solve kernels.  Matrices are staged unpadded (leading dimension n) in
-// shared memory: transpose products use one warp per output column with the
-// lanes along the contraction (conflict-free, shuffle reduction); normal
-// products use one thread per output row.
+// solve kernels.  Per chain step the three factor blocks (V_i, W, Y_i) are
+// staged unpadded (leading dimension n) in shared memory with cp.async, the
+// next step's blocks streaming into the other half of a double buffer while
+// the current step computes.  Transpose products (M^T v) use one warp per
+// output column with the lanes along the contraction (conflict-free,
+// shuffle reduction); normal products (M v) use one thread per output row,
+// the contraction split over thread groups and reduced through smem.
 // ---------------------------------------------------------------------------
 constexpr int SOLVE_THREADS = 256;
 
-template <class Tg, class T>
-__device__ __forceinline__ void stage_matrix(T *s, const Tg *__restrict__ g, long long nn)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
-    for (long long e = threadIdx.x; e < nn; e += blockDim.x) s[e] = (T)g[e];
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// async copy of `count` contiguous elements (both ends aligned to 16 B when
+// count*sizeof(T) is a multiple of 16, which the caller's layout guarantees)
+template <class T>
+__device__ __forceinline__ void async_copy(T *s, const T *__restrict__ g, int count)
+{
+    if (((count * (int)sizeof(T)) & 15) == 0) {
+        const int chunks = count * (int)sizeof(T) / 16;
+        for (int e = threadIdx.x; e < chunks; e += blockDim.x)
+            cp_async16(reinterpret_cast<char *>(s) + 16 * e, reinterpret_cast<const char *>(g) + 16 * e);
+    } else {
+        for (int e = threadIdx.x; e < count; e += blockDim.x) {
+            if (sizeof(T) == 8)
+                cp_async8(s + e, g + e);
+            else
+                cp_async4(s + e, g + e);
+        }
+    }
 }
 
 // out(c, j) (+)= sign * sum_r M(r, c) v(r, j); M n x n (ld n), v/out n x kc (ld n)
@@ -525,31 +650,31 @@ __device__ __forceinline__ void cta_tmul(const T *sM, const T *v, T *out, int n,
     }
 }
 
-// out(r, j) = acc(r, j) - sum_c M1(r,c) v1(c,j) [- sum_c M2(r,c) v2(c,j)]
+// out(r, j) = base(r, j) + sign * (sum_c M1(r,c) v1(c,j) [+ sum_c M2(r,c) v2(c,j)])
+// (base may be null).  `red` holds max(blockDim, n*kc) elements.  Ends
+// without a barrier; callers sync before reading `out`.
 template <class T>
-__device__ __forceinline__ void cta_nmul_sub(const T *sM1, const T *v1, const T *sM2, const T *v2, T *io, int n,
-                                             int kc)
+__device__ __forceinline__ void cta_nmul(const T *M1, const T *v1, const T *M2, const T *v2, const T *base, T *out,
+                                         T sign, int n, int kc, T *red)
 {
-    for (int o = threadIdx.x; o < n * kc; o += blockDim.x) {
-        const int r = o % n, j = o / n;
-        T s = io[o];
-        if (sM1)
-            for (int c = 0; c < n; ++c) s = fma(-sM1[r + c * n], v1[c + j * n], s);
-        if (sM2)
-            for (int c = 0; c < n; ++c) s = fma(-sM2[r + c * n], v2[c + j * n], s);
-        io[o] = s;
-    }
-}
-
-// out(r, j) = sum_c M(r,c) v(c,j)
-template <class T>
-__device__ __forceinline__ void cta_nmul(const T *sM, const T *v, T *out, int n, int kc)
-{
-    for (int o = threadIdx.x; o < n * kc; o += blockDim.x) {
-        const int r = o % n, j = o / n;
+    const int no = n * kc;
+    int parts = (int)blockDim.x / no;
+    parts = parts < 1 ? 1 : (parts > 8 ? 8 : parts);
+    for (int w = threadIdx.x; w < parts * no; w += blockDim.x) {
+        const int part = w / no, o = w - part * no;
+        const int j = o / n, r = o - j * n;
+        const int c0 = (part * n) / parts, c1 = ((part + 1) * n) / parts;
         T s = T(0);
-        for (int c = 0; c < n; ++c) s = fma(sM[r + c * n], v[c + j * n], s);
-        out[o] = s;
+        for (int c = c0; c < c1; ++c) s = fma(M1[r + c * n], v1[c + j * n], s);
+        if (M2)
+            for (int c = c0; c < c1; ++c) s = fma(M2[r + c * n], v2[c + j * n], s);
+        red[w] = s;
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < no; o += blockDim.x) {
+        T s = T(0);
+        for (int q = 0; q < parts; ++q) s += red[q * no + o];
+        out[o] = (base ? base[o] : T(0)) + sign * s;
     }
 }
 
@@ -558,7 +683,7 @@ struct SolveArgs {
     const T *Af;   // V per block
     const T *Bf;   // W per block
     const T *Y;    // left fill per block (null when seq)
-    T *d;          // level RHS (N blocks, ld_blk = n*k elements per block); y / x in place
+    T *d;          // level RHS (N blocks, n*k elements per block); y / x in place
     T *bvec;       // Q x [bL | bR] (n x kc each, per column chunk)
     const void *xsep;  // next-level solution (Q+1 blocks, n x k each), type Tsep
     long long N;
@@ -570,10 +695,11 @@ struct SolveArgs {
     int seq;
 };
 
+// shared memory: 2 buffers x 3 blocks + 5 vectors + reduction scratch
 template <class T>
 __host__ __device__ constexpr size_t solve_smem_bytes(int n, int kc)
 {
-    return (size_t)(3 * n * n + 5 * n * kc) * sizeof(T);
+    return (size_t)(6 * n * n + 5 * n * kc + (n * kc > SOLVE_THREADS ? n * kc : SOLVE_THREADS)) * sizeof(T);
 }
 
 // load n x kc columns j0.. of block blk of a (n x k per block) tensor
@@ -590,22 +716,21 @@ __device__ __forceinline__ void store_rhs(Tg *__restrict__ g, const T *s, long l
     for (int e = threadIdx.x; e < n * kc; e += blockDim.x) b[e] = (Tg)s[e];
 }
 
-// forward sweep of one partition (or the whole chain when seq, followed by
-// the backward sweep: the coarsest-level sequential solve).
+// forward sweep of one partition; for the sequential (coarsest) level the
+// whole chain followed by its backward sweep.
 template <class T>
 __global__ void __launch_bounds__(SOLVE_THREADS) chain_fwd_kernel(SolveArgs<T> g)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = g.n, kc = g.kc;
-    const long long nn = (long long)n * n;
-    T *sV = reinterpret_cast<T *>(smem_raw);
-    T *sW = sV + nn;
-    T *sY = sW + nn;
-    T *sr = sY + nn;
+    const int nn = n * n;
+    T *buf = reinterpret_cast<T *>(smem_raw);  // [2][3][nn]: V, W, Y
+    T *sr = buf + 6 * nn;
     T *sy = sr + n * kc;
     T *sbL = sy + n * kc;
     T *sbR = sbL + n * kc;
     T *sx = sbR + n * kc;
+    T *red = sx + n * kc;
     const bool seq = g.seq != 0;
     const long long p = blockIdx.x;
     long long first, last;
@@ -619,27 +744,35 @@ __global__ void __launch_bounds__(SOLVE_THREADS) chain_fwd_kernel(SolveArgs<T> g
         last = sR - 1;
     }
     for (int e = threadIdx.x; e < n * kc; e += blockDim.x) sbL[e] = T(0);
-
+    // step i uses V_i (slot 0), W_{i-1} (slot 1), Y_i (slot 2) in buffer (i - first) & 1
+    async_copy(buf, g.Af + first * (long long)nn, nn);
+    if (!seq) async_copy(buf + 2 * nn, g.Y + first * (long long)nn, nn);
+    cp_async_commit();
     for (long long i = first; i <= last; ++i) {
-        stage_matrix(sV, g.Af + i * nn, nn);
-        if (i > first) stage_matrix(sW, g.Bf + (i - 1) * nn, nn);
-        if (!seq) stage_matrix(sY, g.Y + i * nn, nn);
+        T *cur = buf + ((i - first) & 1) * 3 * nn;
+        T *nxt = buf + (((i - first) & 1) ^ 1) * 3 * nn;
         load_rhs(sr, g.d, i, n, g.k, g.j0, kc);
+        cp_async_wait_all();
         __syncthreads();
+        // prefetch step i+1 (W_i is also what bR needs after the last step)
+        if (i < last) async_copy(nxt, g.Af + (i + 1) * (long long)nn, nn);
+        if (!seq || i < last) async_copy(nxt + nn, g.Bf + i * (long long)nn, nn);
+        if (!seq && i < last) async_copy(nxt + 2 * nn, g.Y + (i + 1) * (long long)nn, nn);
+        cp_async_commit();
         if (i > first) {
-            cta_tmul(sW, sy, sr, n, kc, T(-1), true);
+            cta_tmul(cur + nn, sy, sr, n, kc, T(-1), true);
             __syncthreads();
         }
-        cta_tmul(sV, sr, sy, n, kc, T(1), false);
+        cta_tmul(cur, sr, sy, n, kc, T(1), false);
         __syncthreads();
-        if (!seq) cta_tmul(sY, sy, sbL, n, kc, T(1), true);
+        if (!seq) cta_tmul(cur + 2 * nn, sy, sbL, n, kc, T(1), true);
         store_rhs(g.d, sy, i, n, g.k, g.j0, kc);
-        __syncthreads();
     }
+    cp_async_wait_all();
+    __syncthreads();
     if (!seq) {
-        stage_matrix(sW, g.Bf + last * nn, nn);
-        __syncthreads();
-        cta_tmul(sW, sy, sbR, n, kc, T(1), false);
+        const T *wl = buf + (((last + 1 - first) & 1) * 3 + 1) * nn;  // W_last, prefetched in the last step
+        cta_tmul(wl, sy, sbR, n, kc, T(1), false);
         __syncthreads();
         T *bp = g.bvec + p * 2 * (long long)n * kc;
         for (int e = threadIdx.x; e < n * kc; e += blockDim.x) {
@@ -648,21 +781,30 @@ __global__ void __launch_bounds__(SOLVE_THREADS) chain_fwd_kernel(SolveArgs<T> g
         }
         return;
     }
-    // sequential level: backward sweep x_i = V_i (y_i - W_i x_{i+1})
+    // sequential level, backward: x_i = V_i (y_i - W_i x_{i+1}); step i uses
+    // V_i (slot 0) and W_i (slot 1)
+    async_copy(buf, g.Af + last * (long long)nn, nn);
+    cp_async_commit();
     for (long long i = last; i >= first; --i) {
-        stage_matrix(sV, g.Af + i * nn, nn);
-        if (i < last) stage_matrix(sW, g.Bf + i * nn, nn);
+        T *cur = buf + ((last - i) & 1) * 3 * nn;
+        T *nxt = buf + (((last - i) & 1) ^ 1) * 3 * nn;
         load_rhs(sr, g.d, i, n, g.k, g.j0, kc);
+        cp_async_wait_all();
         __syncthreads();
+        if (i > first) {
+            async_copy(nxt, g.Af + (i - 1) * (long long)nn, nn);
+            async_copy(nxt + nn, g.Bf + (i - 1) * (long long)nn, nn);
+        }
+        cp_async_commit();
         if (i < last) {
-            cta_nmul_sub<T>(sW, sx, nullptr, nullptr, sr, n, kc);
+            cta_nmul<T>(cur + nn, sx, nullptr, nullptr, sr, sr, T(-1), n, kc, red);
             __syncthreads();
         }
-        cta_nmul(sV, sr, sx, n, kc);
+        cta_nmul<T>(cur, sr, nullptr, nullptr, nullptr, sx, T(1), n, kc, red);
         __syncthreads();
         store_rhs(g.d, sx, i, n, g.k, g.j0, kc);
-        __syncthreads();
     }
+    cp_async_wait_all();
 }
 
 // separator RHS: d'_s = d_{sep s} - bL(s) - bR(s-1)   (reference compute_schur_RHS!,
@@ -694,38 +836,48 @@ __global__ void __launch_bounds__(SOLVE_THREADS) chain_bwd_kernel(SolveArgs<T> g
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = g.n, kc = g.kc;
-    const long long nn = (long long)n * n;
-    T *sV = reinterpret_cast<T *>(smem_raw);
-    T *sW = sV + nn;
-    T *sY = sW + nn;
-    T *sz = sY + nn;
+    const int nn = n * n;
+    T *buf = reinterpret_cast<T *>(smem_raw);  // [2][3][nn]: V_i, W_i, Y_i
+    T *sz = buf + 6 * nn;
     T *sxL = sz + n * kc;
     T *sxn = sxL + n * kc;
     T *sxt = sxn + n * kc;
+    T *red = sxt + 2 * n * kc;
     const long long p = blockIdx.x;
     const long long sL = (p * (g.N - 1)) / g.Q;
     const long long sR = ((p + 1) * (g.N - 1)) / g.Q;
     const long long first = sL + 1, last = sR - 1;
     const Tsep *xs = reinterpret_cast<const Tsep *>(g.xsep);
+    async_copy(buf, g.Af + last * (long long)nn, nn);
+    async_copy(buf + nn, g.Bf + last * (long long)nn, nn);
+    async_copy(buf + 2 * nn, g.Y + last * (long long)nn, nn);
+    cp_async_commit();
     load_rhs(sxL, xs, p, n, g.k, g.j0, kc);
     load_rhs(sxn, xs, p + 1, n, g.k, g.j0, kc);
     __syncthreads();
     store_rhs(g.d, sxL, sL, n, g.k, g.j0, kc);
     if (p == g.Q - 1) store_rhs(g.d, sxn, sR, n, g.k, g.j0, kc);
     for (long long i = last; i >= first; --i) {
-        stage_matrix(sV, g.Af + i * nn, nn);
-        stage_matrix(sW, g.Bf + i * nn, nn);
-        stage_matrix(sY, g.Y + i * nn, nn);
+        T *cur = buf + ((last - i) & 1) * 3 * nn;
+        T *nxt = buf + (((last - i) & 1) ^ 1) * 3 * nn;
         load_rhs(sz, g.d, i, n, g.k, g.j0, kc);
+        cp_async_wait_all();
         __syncthreads();
-        cta_nmul_sub<T>(sY, sxL, sW, sxn, sz, n, kc);
+        if (i > first) {
+            async_copy(nxt, g.Af + (i - 1) * (long long)nn, nn);
+            async_copy(nxt + nn, g.Bf + (i - 1) * (long long)nn, nn);
+            async_copy(nxt + 2 * nn, g.Y + (i - 1) * (long long)nn, nn);
+        }
+        cp_async_commit();
+        cta_nmul<T>(cur + 2 * nn, sxL, cur + nn, sxn, sz, sz, T(-1), n, kc, red);
         __syncthreads();
-        cta_nmul(sV, sz, sxt, n, kc);
+        cta_nmul<T>(cur, sz, nullptr, nullptr, nullptr, sxt, T(1), n, kc, red);
         __syncthreads();
         for (int e = threadIdx.x; e < n * kc; e += blockDim.x) sxn[e] = sxt[e];
         store_rhs(g.d, sxt, i, n, g.k, g.j0, kc);
         __syncthreads();
     }
+    cp_async_wait_all();
 }
 
 // ---------------------------------------------------------------------------

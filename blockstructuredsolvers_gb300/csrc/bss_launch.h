@@ -47,4 +47,8 @@ cudaError_t launch_init_identity(T *A, long long first_blk, long long last_blk, 
 
 int solve_kc_max(int n, int k, int elem_bytes);
 
+// process-wide count of kernels this library launched (all handles)
+void count_launch();
+long long launch_count();
+
 }  // namespace bss

@@ -22,6 +22,7 @@ static cudaError_t chain_factor_nb(const ChainFactorArgs<Tin, T> &a, cudaStream_
     if (e != cudaSuccess) return e;
     const unsigned grid = a.seq ? 1u : (unsigned)a.Q;
     kern<<<grid, Tile<NB>::THREADS, smem, s>>>(a);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -64,6 +65,7 @@ cudaError_t launch_assemble_schur(const Tsrc *A_src, const T *C, Tdst *A_next, T
 {
     const long long work = (2 * Q + 1) * (long long)n * n;
     assemble_schur_kernel<Tsrc, T, Tdst><<<grid_for(work, 256), 256, 0, s>>>(A_src, C, A_next, B_next, N, Q, n);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -82,6 +84,7 @@ cudaError_t launch_chain_fwd(const SolveArgs<T> &a, cudaStream_t s)
     if (e != cudaSuccess) return e;
     const unsigned grid = a.seq ? 1u : (unsigned)a.Q;
     kern<<<grid, SOLVE_THREADS, smem, s>>>(a);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -93,6 +96,7 @@ cudaError_t launch_chain_bwd(const SolveArgs<T> &a, cudaStream_t s)
     cudaError_t e = set_solve_smem<T>((const void *)kern, smem);
     if (e != cudaSuccess) return e;
     kern<<<(unsigned)a.Q, SOLVE_THREADS, smem, s>>>(a);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -102,6 +106,7 @@ cudaError_t launch_assemble_rhs(const T *d, const T *bvec, Tn *dn, long long N, 
 {
     const long long work = (Q + 1) * (long long)n * kc;
     assemble_rhs_kernel<T, Tn><<<grid_for(work, 256), 256, 0, s>>>(d, bvec, dn, N, Q, n, k, j0, kc);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -109,6 +114,7 @@ template <class T>
 cudaError_t launch_opnorm(const T *A, const T *B, long long N, int n, DevStatus *st, cudaStream_t s)
 {
     opnorm_kernel<T><<<grid_for(N * n, 256), 256, 0, s>>>(A, B, N, n, st);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -116,6 +122,7 @@ template <class T>
 cudaError_t launch_absmax(const T *v, long long count, unsigned long long *dst, cudaStream_t s)
 {
     absmax_kernel<T><<<grid_for(count, 256), 256, 0, s>>>(v, count, dst);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -129,6 +136,7 @@ cudaError_t launch_residual(const T *A, const T *B, const T *x, const T *d, Tr *
     if (e != cudaSuccess) return e;
     int threads = n * k < 256 ? ((n * k + 31) / 32) * 32 : 256;
     kern<<<(unsigned)N, threads, smem, s>>>(A, B, x, d, r, N, n, k, st);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -136,6 +144,7 @@ template <class Tc>
 cudaError_t launch_update(double *x, const Tc *c, long long count, int assign, cudaStream_t s)
 {
     update_kernel<Tc><<<grid_for(count, 256), 256, 0, s>>>(x, c, count, assign);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -143,6 +152,7 @@ template <class Ts, class Td>
 cudaError_t launch_convert(Td *dst, const Ts *src, long long count, cudaStream_t s)
 {
     convert_kernel<Ts, Td><<<grid_for(count, 256), 256, 0, s>>>(dst, src, count);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -152,6 +162,7 @@ cudaError_t launch_init_identity(T *A, long long first_blk, long long last_blk, 
     if (last_blk <= first_blk) return cudaSuccess;
     init_identity_kernel<T><<<grid_for((last_blk - first_blk) * (long long)n * n, 256), 256, 0, s>>>(
         A, first_blk, last_blk, n);
+    count_launch();
     return cudaGetLastError();
 }
 

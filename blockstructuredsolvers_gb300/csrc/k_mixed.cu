@@ -1,5 +1,7 @@
 // Kernel instantiations that cross precisions: FP32 factorization reading
 // FP64 tensors, FP64 residuals written as FP32 corrections, conversions.
+#include <atomic>
+
 #include "bss_launch_impl.cuh"
 
 namespace bss {
@@ -17,9 +19,14 @@ template cudaError_t launch_convert<double, float>(float *, const double *, long
 template cudaError_t launch_convert<double, double>(double *, const double *, long long, cudaStream_t);
 template cudaError_t launch_convert<float, float>(float *, const float *, long long, cudaStream_t);
 
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
 cudaError_t launch_relres(DevStatus *st, double tol, cudaStream_t s)
 {
     relres_kernel<<<1, 32, 0, s>>>(st, tol);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -34,11 +41,15 @@ int tile_for(int n)
 
 int solve_kc_max(int n, int k, int elem_bytes)
 {
-    const long long budget = 200 * 1024;
-    long long kc = (budget / elem_bytes - 3LL * n * n) / (5LL * n);
-    if (kc > 32) kc = 32;
-    if (kc > k) kc = k;
-    if (kc < 1) kc = 1;
-    return (int)kc;
+    // largest column chunk whose double-buffered solve kernels fit in shared memory
+    const long long budget = 220LL * 1024 / elem_bytes;
+    int best = 1;
+    for (int kc = 1; kc <= 32 && kc <= k; ++kc) {
+        const long long nk = (long long)n * kc;
+        const long long need = 6LL * n * n + 5 * nk + (nk > SOLVE_THREADS ? nk : SOLVE_THREADS);
+        if (need > budget) break;
+        best = kc;
+    }
+    return best;
 }
 }  // namespace bss

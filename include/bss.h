@@ -150,6 +150,10 @@ int bss_factorize_levels(bss_handle *h, int32_t nlevels);
 int bss_get_level(bss_handle *h, int32_t level, int64_t *N, int64_t *Q, void **A, void **B, void **d,
                   int32_t *dtype);
 
+/* Number of CUDA kernels this library has launched in this process, over
+ * all handles (no counterpart in the reference; benchmarks report it). */
+int64_t bss_kernel_launches(void);
+
 /* Library build string (kernels compiled, arch). */
 const char *bss_version(void);
 
