@@ -303,20 +303,21 @@ def run_ours(args):
     # ---- e2e through the public API with host buffers ----------------------
     e2e = None
     if not args.quick:
-        Ah = A.permute(2, 0, 1).contiguous().cpu().pin_memory()  # (N, c, r) storage == column-major blocks
-        Bh = B.permute(2, 0, 1).contiguous().cpu().pin_memory()
-        dh = d.permute(2, 0, 1).contiguous().cpu().pin_memory()
+        # host copies in the handle's storage order: (N, c, r) C-order == column-major blocks
+        Ah = A.permute(2, 1, 0).contiguous().cpu().pin_memory()
+        Bh = B.permute(2, 1, 0).contiguous().cpu().pin_memory()
+        dh = d.permute(2, 1, 0).contiguous().cpu().pin_memory()
         xh = torch.empty_like(dh).pin_memory()
         data = bss.initialize_batched(N_BLK, N_SZ, torch.float64, k=K_RHS, precision="mixed")
-        At = data.A_tensor[:, :, :N_BLK].permute(2, 1, 0)  # (N, c, r) view of column-major storage
+        At = data.A_tensor[:, :, :N_BLK].permute(2, 1, 0)  # contiguous (N, c, r) views
         Bt = data.B_tensor[:, :, :N_BLK - 1].permute(2, 1, 0)
         dt = data.d_tensor[:, :, :N_BLK].permute(2, 1, 0)
         ne = max(3, args.steps // 4)
 
         def e2e_step():
-            At.copy_(Ah.permute(0, 2, 1).transpose(1, 2), non_blocking=True)
-            Bt.copy_(Bh.permute(0, 2, 1).transpose(1, 2), non_blocking=True)
-            dt.copy_(dh.permute(0, 2, 1).transpose(1, 2), non_blocking=True)
+            At.copy_(Ah, non_blocking=True)
+            Bt.copy_(Bh, non_blocking=True)
+            dt.copy_(dh, non_blocking=True)
             bss.factorize_(data)
             bss.solve_(data)
             xh.copy_(dt, non_blocking=True)
@@ -331,7 +332,6 @@ def run_ours(args):
         bi = (Ah.numel() + Bh.numel() + dh.numel()) * 8
         bo = xh.numel() * 8
         e2e = {"value": world * ne / te, "unit": "solves/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo}
-        xs = xh.permute(0, 2, 1).numpy()  # math (N, n, k)
         del data
 
     # ---- roofline of the dominant kernel ----------------------------------
