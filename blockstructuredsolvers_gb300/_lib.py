@@ -28,13 +28,15 @@ BSS_PRECISION_PLAIN = 0
 BSS_PRECISION_MIXED = 1
 BSS_PLAN_AUTO = 0
 BSS_PLAN_REFERENCE = 1
+BSS_NOALLOC_SCRATCH_BYTES = 8 << 20
 
 # every entry point include/bss.h declares
 EXPORTS = (
     "bss_default_options", "bss_create_batched", "bss_create_seq", "bss_destroy",
     "bss_get_tensors", "bss_get_dims", "bss_factorize", "bss_solve", "bss_synchronize",
     "bss_get_info", "bss_last_error_string", "bss_plan_reference", "bss_residual",
-    "bss_factorize_levels", "bss_get_level", "bss_kernel_launches", "bss_version",
+    "bss_factorize_levels", "bss_get_level", "bss_factor_solve_noalloc", "bss_kernel_launches",
+    "bss_version",
 )
 
 
@@ -105,6 +107,7 @@ def load(path: str | None = None):
     L.bss_factorize_levels.argtypes = [vp, i32]
     L.bss_get_level.argtypes = [vp, i32, ctypes.POINTER(i64), ctypes.POINTER(i64), ctypes.POINTER(vp),
                                 ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(i32)]
+    L.bss_factor_solve_noalloc.argtypes = [i64, i64, i64, i32, vp, vp, vp, vp]
     L.bss_kernel_launches.argtypes = []
     L.bss_kernel_launches.restype = ctypes.c_int64
     L.bss_version.argtypes = []

@@ -33,6 +33,12 @@ int fail(int code, const std::string &msg)
     return code;
 }
 
+}  // namespace
+
+void bss::set_last_error(const std::string &msg) { g_last_error = msg; }
+
+namespace {
+
 int cuda_fail(cudaError_t e, const char *what)
 {
     return fail(e == cudaErrorMemoryAllocation ? BSS_ERR_OOM : BSS_ERR_CUDA,

@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "bss_kernels.cuh"
 
 namespace bss {
@@ -46,6 +48,9 @@ template <class T>
 cudaError_t launch_init_identity(T *A, long long first_blk, long long last_blk, int n, cudaStream_t s);
 
 int solve_kc_max(int n, int k, int elem_bytes);
+
+// message returned by bss_last_error_string() on this host thread
+void set_last_error(const std::string &msg);
 
 // process-wide count of kernels this library launched (all handles)
 void count_launch();

@@ -150,6 +150,29 @@ int bss_factorize_levels(bss_handle *h, int32_t nlevels);
 int bss_get_level(bss_handle *h, int32_t level, int64_t *N, int64_t *Q, void **A, void **B, void **d,
                   int32_t *dtype);
 
+/* ---- factorize + solve without any device allocation ------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory: hosts whose memory manager owns the whole device pool (a Julia or
+ * MATLAB process that hands out only its own buffers, a serving process
+ * with a fixed memory budget, code running where cudaMalloc is forbidden).
+ * Factors and solves one system in place on CALLER-OWNED device buffers A
+ * (n x n x N), B (n x n x (N-1)) and d (n x k x N), in the dtype's own
+ * precision (like factorize! followed by solve!: A and B hold factors and d
+ * holds x afterwards).  The recursion workspace lives in one file-scope
+ * `static __device__` array of BSS_NOALLOC_SCRATCH_BYTES bytes that every GPU
+ * loading this library reserves until the process exits; this call performs
+ * no cudaMalloc/cudaFree and calls no allocating library routine.  A problem
+ * whose workspace does not fit is rejected with BSS_ERR_ARG before any work
+ * is launched.  The first call on a device looks up the array's device
+ * address with that device current; make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU
+ * (other streams, other host threads) race on it, so serialise them.
+ * Blocks until the stream has finished; returns BSS_ERR_NOT_SPD on a failed
+ * pivot. */
+#define BSS_NOALLOC_SCRATCH_BYTES (8u << 20)
+int bss_factor_solve_noalloc(int64_t N, int64_t n, int64_t k, int32_t dtype, void *A, void *B, void *d,
+                             void *stream);
+
 /* Number of CUDA kernels this library has launched in this process, over
  * all handles (no counterpart in the reference; benchmarks report it). */
 int64_t bss_kernel_launches(void);
