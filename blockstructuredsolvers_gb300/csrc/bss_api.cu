@@ -88,6 +88,7 @@ struct bss_handle {
     DevStatus *st = nullptr;
     DevStatus *h_st = nullptr;  // pinned mirror
     bool factored = false;
+    bool need_anorm = false;  // the next residual also computes ||T||_inf
     int kc_max = 1;
     bss_info info{};
     int sticky = BSS_OK;
@@ -254,7 +255,9 @@ int build_handle(bss_handle *h)
             long long target = h->opt.target_partitions > 0
                                    ? h->opt.target_partitions
                                    : (long long)sms * chain_ctas_per_sm(tin0, t0, (int)n);
-            long long cutoff = h->opt.seq_cutoff > 0 ? h->opt.seq_cutoff : 8;
+            // mixed: the coarsest level is FP64, whose per-SM rate is ~1/64 of FP32,
+            // so halve down to 2 blocks; plain: 4 balances levels against chain length
+            long long cutoff = h->opt.seq_cutoff > 0 ? h->opt.seq_cutoff : (mixed ? 2 : 4);
             plan_auto(h->N, target, cutoff, Ns, Qs, coarsest);
         }
     }
@@ -538,9 +541,9 @@ static int factorize_upto(bss_handle *h, int upto)
     BSS_CUDA(cudaMemsetAsync(&h->st->bad_key, 0xFF, sizeof(unsigned long long), h->stream));
     const bool mixed = h->opt.precision == BSS_PRECISION_MIXED;
     if (mixed) {
+        // ||T||_inf is folded into the first residual after this factorization
         BSS_CUDA(cudaMemsetAsync(&h->st->anorm, 0, sizeof(unsigned long long), h->stream));
-        BSS_CUDA(launch_opnorm<double>((const double *)h->A, (const double *)h->B, h->N, (int)h->n, h->st,
-                                       h->stream));
+        h->need_anorm = true;
     }
     const int nlev = (int)h->levels.size();
     for (int l = 0; l < nlev && l < upto; ++l) {
@@ -679,12 +682,16 @@ int solve_mixed(bss_handle *h)
     bool converged = false;
     for (int it = 0; it <= h->opt.max_refine; ++it) {
         BSS_CUDA(cudaMemsetAsync(&st->rnorm, 0, 2 * sizeof(unsigned long long), h->stream));
+        const int wn = h->need_anorm ? 1 : 0;
+        h->need_anorm = false;
         if (c_is_f32)
             BSS_CUDA((launch_residual<double, float>((const double *)h->A, (const double *)h->B, h->x64, d64,
-                                                     (float *)h->c0, h->N, (int)h->n, (int)h->k, st, h->stream)));
+                                                     (float *)h->c0, h->N, (int)h->n, (int)h->k, wn, st,
+                                                     h->stream)));
         else
             BSS_CUDA((launch_residual<double, double>((const double *)h->A, (const double *)h->B, h->x64, d64,
-                                                      (double *)h->c0, h->N, (int)h->n, (int)h->k, st, h->stream)));
+                                                      (double *)h->c0, h->N, (int)h->n, (int)h->k, wn, st,
+                                                      h->stream)));
         BSS_CUDA(launch_relres(st, h->opt.tol, h->stream));
         BSS_CUDA(cudaMemcpyAsync(h->h_st, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->stream));
         BSS_CUDA(cudaStreamSynchronize(h->stream));
@@ -757,17 +764,15 @@ extern "C" int bss_residual(int64_t N, int64_t n, int64_t k, int32_t dtype, cons
     const long long cnt = N * n * k;
     cudaError_t e;
     if (dtype == BSS_F64) {
-        e = launch_opnorm<double>((const double *)A, (const double *)B, N, (int)n, st, s);
-        if (e == cudaSuccess) e = launch_absmax<double>((const double *)d, cnt, &st->dnorm, s);
+        e = launch_absmax<double>((const double *)d, cnt, &st->dnorm, s);
         if (e == cudaSuccess)
             e = launch_residual<double, double>((const double *)A, (const double *)B, (const double *)x,
-                                                (const double *)d, nullptr, N, (int)n, (int)k, st, s);
+                                                (const double *)d, nullptr, N, (int)n, (int)k, 1, st, s);
     } else {
-        e = launch_opnorm<float>((const float *)A, (const float *)B, N, (int)n, st, s);
-        if (e == cudaSuccess) e = launch_absmax<float>((const float *)d, cnt, &st->dnorm, s);
+        e = launch_absmax<float>((const float *)d, cnt, &st->dnorm, s);
         if (e == cudaSuccess)
             e = launch_residual<float, float>((const float *)A, (const float *)B, (const float *)x, (const float *)d,
-                                              nullptr, N, (int)n, (int)k, st, s);
+                                              nullptr, N, (int)n, (int)k, 1, st, s);
     }
     if (e == cudaSuccess) e = launch_relres(st, 0.0, s);
     DevStatus hs;

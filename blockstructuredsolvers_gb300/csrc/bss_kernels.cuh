@@ -119,30 +119,44 @@ __device__ __forceinline__ void fma_vec(double &acc, const double2 &x, const dou
 }
 
 // acc[a][b] += sum_k X(k, ti+TI*a) * Y(k, tj+TJ*b)     (C += X^T Y)
-template <class T, int NB>
-__device__ __forceinline__ void tn_acc(T (&acc)[Tile<NB>::RA][Tile<NB>::RB], const T *X, const T *Y,
-                                       int ti, int tj)
+// Structure flags (all decided at compile time, per 16-row segment of k):
+//   TRI : X is upper triangular, so X(k, i) = 0 for k > i; in k-segment s only
+//         rows with a >= s contribute (row ti+16a < 16s otherwise).
+//   SYM : only C's upper block pairs a <= b are needed (symmetric result).
+enum { TN_FULL = 0, TN_TRI = 1, TN_SYM = 2 };
+
+template <class T, int NB, int F1>
+__device__ __forceinline__ void tn_acc(T (&acc)[Tile<NB>::RA][Tile<NB>::RB], const T *X, const T *Y, int ti, int tj)
 {
     using TL = Tile<NB>;
     using V = typename Vec<T>::type;
     constexpr int LD = Geo<T, NB>::LD;
     constexpr int W = Vec<T>::W;
-#pragma unroll 4
-    for (int k = 0; k < NB; k += W) {
-        V xa[TL::RA], yb[TL::RB];
+    static_assert(TL::TI == 16, "segments are 16 rows");
 #pragma unroll
-        for (int a = 0; a < TL::RA; ++a) xa[a] = *reinterpret_cast<const V *>(X + k + (ti + TL::TI * a) * LD);
+    for (int seg = 0; seg < NB / 16; ++seg) {
+#pragma unroll 2
+        for (int kk = 0; kk < 16; kk += W) {
+            const int k = 16 * seg + kk;
+            V xa[TL::RA], yb[TL::RB];
 #pragma unroll
-        for (int b = 0; b < TL::RB; ++b) yb[b] = *reinterpret_cast<const V *>(Y + k + (tj + TL::TJ * b) * LD);
+            for (int a = 0; a < TL::RA; ++a)
+                if (!(F1 & TN_TRI) || a >= seg) xa[a] = *reinterpret_cast<const V *>(X + k + (ti + TL::TI * a) * LD);
 #pragma unroll
-        for (int a = 0; a < TL::RA; ++a)
+            for (int b = 0; b < TL::RB; ++b) yb[b] = *reinterpret_cast<const V *>(Y + k + (tj + TL::TJ * b) * LD);
 #pragma unroll
-            for (int b = 0; b < TL::RB; ++b) fma_vec(acc[a][b], xa[a], yb[b]);
+            for (int a = 0; a < TL::RA; ++a)
+#pragma unroll
+                for (int b = 0; b < TL::RB; ++b)
+                    if ((!(F1 & TN_TRI) || a >= seg) && (!(F1 & TN_SYM) || (TL::TI * a <= TL::TJ * b + TL::TJ - 1)))
+                        fma_vec(acc[a][b], xa[a], yb[b]);
+        }
     }
 }
 
-// acc1 += X^T Y1, acc2 += X^T Y2 (shared X reads)
-template <class T, int NB>
+// acc1 += X^T Y1 (flags F1), acc2 += X^T Y2 (flags F2), shared X reads.
+// TRI applies to X and so must be given to both or neither.
+template <class T, int NB, int F1, int F2>
 __device__ __forceinline__ void tn_acc2(T (&acc1)[Tile<NB>::RA][Tile<NB>::RB],
                                         T (&acc2)[Tile<NB>::RA][Tile<NB>::RB], const T *X, const T *Y1,
                                         const T *Y2, int ti, int tj)
@@ -151,24 +165,55 @@ __device__ __forceinline__ void tn_acc2(T (&acc1)[Tile<NB>::RA][Tile<NB>::RB],
     using V = typename Vec<T>::type;
     constexpr int LD = Geo<T, NB>::LD;
     constexpr int W = Vec<T>::W;
+    static_assert(TL::TI == 16, "segments are 16 rows");
+    static_assert((F1 & TN_TRI) == (F2 & TN_TRI), "TRI describes X");
+#pragma unroll
+    for (int seg = 0; seg < NB / 16; ++seg) {
 #pragma unroll 2
-    for (int k = 0; k < NB; k += W) {
-        V xa[TL::RA], yb[TL::RB], zb[TL::RB];
+        for (int kk = 0; kk < 16; kk += W) {
+            const int k = 16 * seg + kk;
+            V xa[TL::RA], yb[TL::RB], zb[TL::RB];
 #pragma unroll
-        for (int a = 0; a < TL::RA; ++a) xa[a] = *reinterpret_cast<const V *>(X + k + (ti + TL::TI * a) * LD);
-#pragma unroll
-        for (int b = 0; b < TL::RB; ++b) {
-            yb[b] = *reinterpret_cast<const V *>(Y1 + k + (tj + TL::TJ * b) * LD);
-            zb[b] = *reinterpret_cast<const V *>(Y2 + k + (tj + TL::TJ * b) * LD);
-        }
-#pragma unroll
-        for (int a = 0; a < TL::RA; ++a)
+            for (int a = 0; a < TL::RA; ++a)
+                if (!(F1 & TN_TRI) || a >= seg) xa[a] = *reinterpret_cast<const V *>(X + k + (ti + TL::TI * a) * LD);
 #pragma unroll
             for (int b = 0; b < TL::RB; ++b) {
-                fma_vec(acc1[a][b], xa[a], yb[b]);
-                fma_vec(acc2[a][b], xa[a], zb[b]);
+                yb[b] = *reinterpret_cast<const V *>(Y1 + k + (tj + TL::TJ * b) * LD);
+                zb[b] = *reinterpret_cast<const V *>(Y2 + k + (tj + TL::TJ * b) * LD);
             }
+#pragma unroll
+            for (int a = 0; a < TL::RA; ++a)
+#pragma unroll
+                for (int b = 0; b < TL::RB; ++b) {
+                    if (!(F1 & TN_TRI) || a >= seg) {
+                        if (!(F1 & TN_SYM) || (TL::TI * a <= TL::TJ * b + TL::TJ - 1)) fma_vec(acc1[a][b], xa[a], yb[b]);
+                        if (!(F2 & TN_SYM) || (TL::TI * a <= TL::TJ * b + TL::TJ - 1)) fma_vec(acc2[a][b], xa[a], zb[b]);
+                    }
+                }
+        }
     }
+}
+
+// store a symmetric result computed on its upper block pairs: element
+// (r, c) of every computed pair, plus its mirror (c, r) when the whole pair
+// lies above the diagonal
+template <class T, int NB>
+__device__ __forceinline__ void store_sym_global(T *__restrict__ g, const T (&src)[Tile<NB>::RA][Tile<NB>::RB], int n,
+                                                 int ti, int tj)
+{
+    using TL = Tile<NB>;
+#pragma unroll
+    for (int a = 0; a < TL::RA; ++a)
+#pragma unroll
+        for (int b = 0; b < TL::RB; ++b) {
+            const int r = ti + TL::TI * a, c = tj + TL::TJ * b;
+            if (TL::TI * a > TL::TJ * b + TL::TJ - 1) continue;         // pair not computed
+            const bool strictly_upper = (TL::TI * a + TL::TI - 1 < TL::TJ * b);  // every element r < c
+            if (r < n && c < n) {
+                g[r + (size_t)c * n] = src[a][b];
+                if (strictly_upper) g[c + (size_t)r * n] = src[a][b];
+            }
+        }
 }
 
 template <class T, int NB>
@@ -239,33 +284,53 @@ __device__ __forceinline__ T safe_pivot(T p)
 // in the reference's backbone_cpu.jl:7,13 / cusolverDnXpotrf(Batched) 'U').
 // On exit sS's upper triangle holds U (U^T U = S), its lower triangle is
 // scratch, and sV holds V = U^{-1} (upper, zeros below the diagonal -- the
-// caller zeroes sV's strictly lower 16x16 tiles once).
-// Panels are PB = 16 wide: one warp factors each 16x16 diagonal tile with
-// shuffles (lane r owns column r), another warp inverts it by per-lane back
-// substitution while the rest of the CTA solves the row panel; the trailing
-// matrix update and the NB/16-1 block stages of V are spread over the CTA.
+// caller zeroes sV's strictly lower tiles once).
+// Panels are PB = 16 wide: one warp factors each
+// PB x PB diagonal tile with shuffles (lane r owns column r; the diagonal is
+// carried in its own register so the pivot chain is shuffle -> rsqrt -> fma),
+// another warp inverts it by per-lane back substitution while the rest of
+// the CTA solves the row panel; the trailing update and the NB/PB-1 block
+// stages of V are spread over the CTA.  The helpers are kept out of line:
+// inlined together into the chain kernel they push arrays to local memory.
 // ---------------------------------------------------------------------------
-constexpr int PB = 16;
 
-template <class T, int LD>
-__device__ __forceinline__ int warp_chol16(T *sS, T *dinv, int o, int lane)
+// 1/sqrt of a pivot: the hardware approximation in FP32 (2 ulp; FP32
+// factors are refined in FP64 or checked at 1e-4), IEEE sqrt and divide in FP64
+__device__ __forceinline__ float rsqrt_pivot(float p) { return rsqrtf(p); }
+__device__ __forceinline__ double rsqrt_pivot(double p) { return 1.0 / sqrt(p); }
+
+// 16-wide panels measured faster than 32-wide ones on GB300 for NB = 64
+// (24k vs 30k cycles per 64x64 factorization in one CTA): the warp
+// factorization of a diagonal tile is bound by shuffle issue, which grows
+// with the panel width, and the 32x32 inverse stage costs more than three
+// 16x16 ones.
+template <int NB>
+struct Panel {
+    static constexpr int PB = 16;
+};
+
+template <class T, int LD, int PB>
+__device__ __noinline__ int warp_chol(T *sS, T *dinv, int o, int lane)
 {
     const int r = lane & (PB - 1);
     T u[PB];
 #pragma unroll
     for (int c = 0; c < PB; ++c) u[c] = sS[(o + c) + (o + r) * LD];  // S(o+c, o+r), valid for c <= r
+    T diag = sS[(o + r) + (o + r) * LD];
     int bad = 0;
     T udiag = T(1);
 #pragma unroll
     for (int j = 0; j < PB; ++j) {
-        T piv = __shfl_sync(0xffffffffu, u[j], j);
+        T piv = __shfl_sync(0xffffffffu, diag, j);
         if (!(piv > T(0) && piv < T(INFINITY))) {
             bad = 1;
             piv = T(1);
         }
-        const T ujr = u[j] * (T(1) / sqrt(piv));  // U(j, r), r >= j
-        u[j] = ujr;
+        const T rs = rsqrt_pivot(piv);
+        const T ujr = (r == j ? diag : u[j]) * rs;  // U(j, r) for r >= j
         if (j == r) udiag = ujr;
+        diag = fma(-ujr, ujr, diag);                // own column's diagonal: the pivot chain
+        u[j] = ujr;
 #pragma unroll
         for (int c = j + 1; c < PB; ++c) {
             const T ujc = __shfl_sync(0xffffffffu, ujr, c);  // U(j, c) from lane c
@@ -275,15 +340,15 @@ __device__ __forceinline__ int warp_chol16(T *sS, T *dinv, int o, int lane)
     if (lane < PB) {
 #pragma unroll
         for (int c = 0; c < PB; ++c)
-            if (c <= r) sS[(o + c) + (o + r) * LD] = u[c];
+            if (c <= r) sS[(o + c) + (o + r) * LD] = (c == r) ? udiag : u[c];
         dinv[o + r] = T(1) / udiag;
     }
     return bad;
 }
 
 // V_KK = U_KK^{-1}: lane r computes column r by back substitution.
-template <class T, int LD>
-__device__ __forceinline__ void warp_inv16(const T *sS, const T *dinv, T *sV, int o, int lane)
+template <class T, int LD, int PB>
+__device__ __noinline__ void warp_inv(const T *sS, const T *dinv, T *sV, int o, int lane)
 {
     const int r = lane & (PB - 1);
     T v[PB];
@@ -305,9 +370,9 @@ __device__ __forceinline__ void warp_inv16(const T *sS, const T *dinv, T *sV, in
     }
 }
 
-// row panel right of diagonal tile o: U(o:o+16, c) = U_KK^{-T} S(o:o+16, c)
-template <class T, int LD, int NB>
-__device__ __forceinline__ void panel_trsm(T *sS, const T *dinv, int o, int t0, int nthr)
+// row panel right of diagonal tile o: U(o:o+PB, c) = U_KK^{-T} S(o:o+PB, c)
+template <class T, int LD, int NB, int PB>
+__device__ __noinline__ void panel_trsm(T *sS, const T *dinv, int o, int t0, int nthr)
 {
     for (int c = o + PB + t0; c < NB; c += nthr) {
         T x[PB];
@@ -324,9 +389,9 @@ __device__ __forceinline__ void panel_trsm(T *sS, const T *dinv, int o, int t0, 
     }
 }
 
-// S(a, b) -= sum_p U(o+p, a) U(o+p, b)   for o+16 <= a <= b < NB
-template <class T, int LD, int NB>
-__device__ __forceinline__ void trailing_update(T *sS, int o, int tid, int nthr)
+// S(a, b) -= sum_p U(o+p, a) U(o+p, b)   for o+PB <= a <= b < NB
+template <class T, int LD, int NB, int PB>
+__device__ __noinline__ void trailing_update(T *sS, int o, int tid, int nthr)
 {
     using V = typename Vec<T>::type;
     constexpr int W = Vec<T>::W;
@@ -350,8 +415,8 @@ __device__ __forceinline__ void trailing_update(T *sS, int o, int tid, int nthr)
 // off-diagonal tiles of V = U^{-1}:  V_IJ = -V_II sum_{P=I+1..J} U_IP V_PJ,
 // one super-diagonal stage at a time (s = J - I).  T_IJ is kept in the
 // (scratch) lower tile (J, I) of sS.
-template <class T, int LD, int NB>
-__device__ __forceinline__ void inverse_stages(T *sS, T *sV, int tid, int nthr)
+template <class T, int LD, int NB, int PB>
+__device__ __noinline__ void inverse_stages(T *sS, T *sV, int tid, int nthr)
 {
     constexpr int KP = NB / PB;
 #pragma unroll 1
@@ -361,23 +426,29 @@ __device__ __forceinline__ void inverse_stages(T *sS, T *sV, int tid, int nthr)
             const int tile = e / (PB * PB), w = e - tile * PB * PB;
             const int a = w % PB, b = w / PB;
             const int I = tile, J = tile + s;
-            T acc = T(0);
+            T acc0 = T(0), acc1 = T(0);
             for (int P = I + 1; P <= J; ++P)
 #pragma unroll
-                for (int q = 0; q < PB; ++q)
-                    acc = fma(sS[(PB * I + a) + (PB * P + q) * LD], sV[(PB * P + q) + (PB * J + b) * LD], acc);
-            sS[(PB * J + a) + (PB * I + b) * LD] = acc;
+                for (int q = 0; q < PB; q += 2) {
+                    acc0 = fma(sS[(PB * I + a) + (PB * P + q) * LD], sV[(PB * P + q) + (PB * J + b) * LD], acc0);
+                    acc1 = fma(sS[(PB * I + a) + (PB * P + q + 1) * LD], sV[(PB * P + q + 1) + (PB * J + b) * LD],
+                               acc1);
+                }
+            sS[(PB * J + a) + (PB * I + b) * LD] = acc0 + acc1;
         }
         __syncthreads();
         for (int e = tid; e < ntile * PB * PB; e += nthr) {
             const int tile = e / (PB * PB), w = e - tile * PB * PB;
             const int a = w % PB, b = w / PB;
             const int I = tile, J = tile + s;
-            T acc = T(0);
-#pragma unroll
-            for (int c = 0; c < PB; ++c)
-                if (c >= a) acc = fma(sV[(PB * I + a) + (PB * I + c) * LD], sS[(PB * J + c) + (PB * I + b) * LD], acc);
-            sV[(PB * I + a) + (PB * J + b) * LD] = -acc;
+            T acc0 = T(0), acc1 = T(0);
+            for (int c = a; c < PB; c += 2) {
+                acc0 = fma(sV[(PB * I + a) + (PB * I + c) * LD], sS[(PB * J + c) + (PB * I + b) * LD], acc0);
+                if (c + 1 < PB)
+                    acc1 = fma(sV[(PB * I + a) + (PB * I + c + 1) * LD], sS[(PB * J + c + 1) + (PB * I + b) * LD],
+                               acc1);
+            }
+            sV[(PB * I + a) + (PB * J + b) * LD] = -(acc0 + acc1);
         }
         __syncthreads();
     }
@@ -389,6 +460,7 @@ template <class T, int NB, int THREADS>
 __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sflag, int tid)
 {
     constexpr int LD = Geo<T, NB>::LD;
+    constexpr int PB = Panel<NB>::PB;
     constexpr int KP = NB / PB;
     const int warp = tid >> 5, lane = tid & 31;
     if (tid == 0) *sflag = 0;
@@ -396,24 +468,24 @@ __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sfla
     for (int K = 0; K < KP; ++K) {
         const int o = PB * K;
         if (warp == 0) {
-            const int bad = warp_chol16<T, LD>(sS, dinv, o, lane);
+            const int bad = warp_chol<T, LD, PB>(sS, dinv, o, lane);
             if (bad && lane == 0) *sflag = 1;
         }
         __syncthreads();
-        if (warp == (THREADS > 32 ? 1 : 0)) warp_inv16<T, LD>(sS, dinv, sV, o, lane);
+        if (warp == (THREADS > 32 ? 1 : 0)) warp_inv<T, LD, PB>(sS, dinv, sV, o, lane);
         if (K + 1 < KP) {
             if (THREADS > 32) {
                 const int t0 = warp == 0 ? lane : tid - 32;
-                if (warp != 1) panel_trsm<T, LD, NB>(sS, dinv, o, t0, THREADS - 32);
+                if (warp != 1) panel_trsm<T, LD, NB, PB>(sS, dinv, o, t0, THREADS - 32);
             } else {
-                panel_trsm<T, LD, NB>(sS, dinv, o, tid, THREADS);
+                panel_trsm<T, LD, NB, PB>(sS, dinv, o, tid, THREADS);
             }
             __syncthreads();
-            trailing_update<T, LD, NB>(sS, o, tid, THREADS);
+            trailing_update<T, LD, NB, PB>(sS, o, tid, THREADS);
         }
         __syncthreads();
     }
-    inverse_stages<T, LD, NB>(sS, sV, tid, THREADS);
+    inverse_stages<T, LD, NB, PB>(sS, sV, tid, THREADS);
     return *sflag;
 }
 
@@ -492,10 +564,10 @@ __global__ void __launch_bounds__(Tile<NB>::THREADS, sizeof(T) == 4 ? 2 : 1) cha
             if (!seq) {
                 T accZ[TL::RA][TL::RB];
                 zero_tile<T, NB>(accZ);
-                tn_acc2<T, NB>(accS, accZ, sW, sW, sY, ti, tj);
+                tn_acc2<T, NB, TN_SYM, TN_FULL>(accS, accZ, sW, sW, sY, ti, tj);
                 store_tile_smem<T, NB>(sZ, accZ, ti, tj, T(-1));
             } else {
-                tn_acc<T, NB>(accS, sW, sW, ti, tj);
+                tn_acc<T, NB, TN_SYM>(accS, sW, sW, ti, tj);
             }
 #pragma unroll
             for (int a = 0; a < TL::RA; ++a)
@@ -519,9 +591,9 @@ __global__ void __launch_bounds__(Tile<NB>::THREADS, sizeof(T) == 4 ? 2 : 1) cha
         zero_tile<T, NB>(accY);
         zero_tile<T, NB>(accW);
         if (!seq)
-            tn_acc2<T, NB>(accY, accW, sV, sZ, sB, ti, tj);
+            tn_acc2<T, NB, TN_TRI, TN_TRI>(accY, accW, sV, sZ, sB, ti, tj);
         else if (has_next)
-            tn_acc<T, NB>(accW, sV, sB, ti, tj);
+            tn_acc<T, NB, TN_TRI>(accW, sV, sB, ti, tj);
 
         // V -> global (coalesced copy from sV)
         {
@@ -541,18 +613,18 @@ __global__ void __launch_bounds__(Tile<NB>::THREADS, sizeof(T) == 4 ? 2 : 1) cha
             store_tile_smem<T, NB>(sY, accY, ti, tj, T(1));
         }
         __syncthreads();
-        if (!seq) tn_acc<T, NB>(accLL, sY, sY, ti, tj);
+        if (!seq) tn_acc<T, NB, TN_SYM>(accLL, sY, sY, ti, tj);
     }
 
     if (!seq) {
         T accRR[TL::RA][TL::RB], accLR[TL::RA][TL::RB];
         zero_tile<T, NB>(accRR);
         zero_tile<T, NB>(accLR);
-        tn_acc<T, NB>(accRR, sW, sW, ti, tj);
-        tn_acc<T, NB>(accLR, sY, sW, ti, tj);
+        tn_acc<T, NB, TN_SYM>(accRR, sW, sW, ti, tj);
+        tn_acc<T, NB, TN_FULL>(accLR, sY, sW, ti, tj);
         T *Cp = g.C + p * 3 * nn;
-        store_tile_global<T, NB>(Cp, accLL, n, ti, tj, T(1));
-        store_tile_global<T, NB>(Cp + nn, accRR, n, ti, tj, T(1));
+        store_sym_global<T, NB>(Cp, accLL, n, ti, tj);
+        store_sym_global<T, NB>(Cp + nn, accRR, n, ti, tj);
         store_tile_global<T, NB>(Cp + 2 * nn, accLR, n, ti, tj, T(1));
     }
 }
@@ -620,7 +692,8 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 template <class T>
 __device__ __forceinline__ void async_copy(T *s, const T *__restrict__ g, int count)
 {
-    if (((count * (int)sizeof(T)) & 15) == 0) {
+    const bool aligned16 = ((((unsigned long long)g) | (unsigned long long)__cvta_generic_to_shared(s)) & 15) == 0;
+    if (aligned16 && ((count * (int)sizeof(T)) & 15) == 0) {
         const int chunks = count * (int)sizeof(T) / 16;
         for (int e = threadIdx.x; e < chunks; e += blockDim.x)
             cp_async16(reinterpret_cast<char *>(s) + 16 * e, reinterpret_cast<const char *>(g) + 16 * e);
@@ -634,18 +707,34 @@ __device__ __forceinline__ void async_copy(T *s, const T *__restrict__ g, int co
     }
 }
 
-// out(c, j) (+)= sign * sum_r M(r, c) v(r, j); M n x n (ld n), v/out n x kc (ld n)
+// out(c, j) (+)= sign * sum_r M(r, c) v(r, j); M n x n (ld n), v/out n x kc (ld n).
+// A warp owns 4 output columns at a time; the four shuffle reductions are
+// interleaved so their latencies overlap.
 template <class T>
 __device__ __forceinline__ void cta_tmul(const T *sM, const T *v, T *out, int n, int kc, T sign, bool accumulate)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int c = warp; c < n; c += nw) {
+    for (int c0 = 4 * warp; c0 < n; c0 += 4 * nw) {
         for (int j = 0; j < kc; ++j) {
-            T s = T(0);
-            for (int r = lane; r < n; r += 32) s = fma(sM[r + c * n], v[r + j * n], s);
+            T s[4] = {T(0), T(0), T(0), T(0)};
+            for (int r = lane; r < n; r += 32) {
+                const T vr = v[r + j * n];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) out[c + j * n] = accumulate ? out[c + j * n] + sign * s : sign * s;
+                for (int q = 0; q < 4; ++q)
+                    if (c0 + q < n) s[q] = fma(sM[r + (c0 + q) * n], vr, s[q]);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
+            if (lane < 4 && c0 + lane < n) {
+                T val = s[0];
+#pragma unroll
+                for (int q = 1; q < 4; ++q)
+                    if (lane == q) val = s[q];
+                const int o = c0 + lane + j * n;
+                out[o] = accumulate ? out[o] + sign * val : sign * val;
+            }
         }
     }
 }
@@ -695,11 +784,17 @@ struct SolveArgs {
     int seq;
 };
 
-// shared memory: 2 buffers x 3 blocks + 5 vectors + reduction scratch
+// shared memory: 2 buffers x 3 blocks + 6 vectors + reduction scratch
 template <class T>
 __host__ __device__ constexpr size_t solve_smem_bytes(int n, int kc)
 {
-    return (size_t)(6 * n * n + 5 * n * kc + (n * kc > SOLVE_THREADS ? n * kc : SOLVE_THREADS)) * sizeof(T);
+    return (size_t)(6 * n * n + 6 * n * kc + (n * kc > SOLVE_THREADS ? n * kc : SOLVE_THREADS)) * sizeof(T);
+}
+
+template <class T>
+__device__ __forceinline__ const T *rhs_ptr(const T *g, long long blk, int n, int k, int j0)
+{
+    return g + blk * (long long)n * k + (long long)j0 * n;
 }
 
 // load n x kc columns j0.. of block blk of a (n x k per block) tensor
@@ -723,14 +818,14 @@ __global__ void __launch_bounds__(SOLVE_THREADS) chain_fwd_kernel(SolveArgs<T> g
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = g.n, kc = g.kc;
-    const int nn = n * n;
+    const int nn = n * n, nkc = n * kc;
     T *buf = reinterpret_cast<T *>(smem_raw);  // [2][3][nn]: V, W, Y
-    T *sr = buf + 6 * nn;
-    T *sy = sr + n * kc;
-    T *sbL = sy + n * kc;
-    T *sbR = sbL + n * kc;
-    T *sx = sbR + n * kc;
-    T *red = sx + n * kc;
+    T *srb = buf + 6 * nn;                     // [2][nkc]: RHS block of the step (prefetched)
+    T *sy = srb + 2 * nkc;
+    T *sbL = sy + nkc;
+    T *sbR = sbL + nkc;
+    T *sx = sbR + nkc;
+    T *red = sx + nkc;
     const bool seq = g.seq != 0;
     const long long p = blockIdx.x;
     long long first, last;
@@ -743,19 +838,24 @@ __global__ void __launch_bounds__(SOLVE_THREADS) chain_fwd_kernel(SolveArgs<T> g
         first = sL + 1;
         last = sR - 1;
     }
-    for (int e = threadIdx.x; e < n * kc; e += blockDim.x) sbL[e] = T(0);
-    // step i uses V_i (slot 0), W_{i-1} (slot 1), Y_i (slot 2) in buffer (i - first) & 1
+    for (int e = threadIdx.x; e < nkc; e += blockDim.x) sbL[e] = T(0);
+    // step i uses V_i (slot 0), W_{i-1} (slot 1), Y_i (slot 2) and d_i in buffer (i - first) & 1
     async_copy(buf, g.Af + first * (long long)nn, nn);
     if (!seq) async_copy(buf + 2 * nn, g.Y + first * (long long)nn, nn);
+    async_copy(srb, rhs_ptr<T>(g.d, first, n, g.k, g.j0), nkc);
     cp_async_commit();
     for (long long i = first; i <= last; ++i) {
-        T *cur = buf + ((i - first) & 1) * 3 * nn;
-        T *nxt = buf + (((i - first) & 1) ^ 1) * 3 * nn;
-        load_rhs(sr, g.d, i, n, g.k, g.j0, kc);
+        const int cb = (int)((i - first) & 1);
+        T *cur = buf + cb * 3 * nn;
+        T *nxt = buf + (cb ^ 1) * 3 * nn;
+        T *sr = srb + cb * nkc;
         cp_async_wait_all();
         __syncthreads();
         // prefetch step i+1 (W_i is also what bR needs after the last step)
-        if (i < last) async_copy(nxt, g.Af + (i + 1) * (long long)nn, nn);
+        if (i < last) {
+            async_copy(nxt, g.Af + (i + 1) * (long long)nn, nn);
+            async_copy(srb + (cb ^ 1) * nkc, rhs_ptr<T>(g.d, i + 1, n, g.k, g.j0), nkc);
+        }
         if (!seq || i < last) async_copy(nxt + nn, g.Bf + i * (long long)nn, nn);
         if (!seq && i < last) async_copy(nxt + 2 * nn, g.Y + (i + 1) * (long long)nn, nn);
         cp_async_commit();
@@ -774,26 +874,29 @@ __global__ void __launch_bounds__(SOLVE_THREADS) chain_fwd_kernel(SolveArgs<T> g
         const T *wl = buf + (((last + 1 - first) & 1) * 3 + 1) * nn;  // W_last, prefetched in the last step
         cta_tmul(wl, sy, sbR, n, kc, T(1), false);
         __syncthreads();
-        T *bp = g.bvec + p * 2 * (long long)n * kc;
-        for (int e = threadIdx.x; e < n * kc; e += blockDim.x) {
+        T *bp = g.bvec + p * 2 * (long long)nkc;
+        for (int e = threadIdx.x; e < nkc; e += blockDim.x) {
             bp[e] = sbL[e];
-            bp[n * kc + e] = sbR[e];
+            bp[nkc + e] = sbR[e];
         }
         return;
     }
     // sequential level, backward: x_i = V_i (y_i - W_i x_{i+1}); step i uses
-    // V_i (slot 0) and W_i (slot 1)
+    // V_i (slot 0), W_i (slot 1) and y_i
     async_copy(buf, g.Af + last * (long long)nn, nn);
+    async_copy(srb, rhs_ptr<T>(g.d, last, n, g.k, g.j0), nkc);
     cp_async_commit();
     for (long long i = last; i >= first; --i) {
-        T *cur = buf + ((last - i) & 1) * 3 * nn;
-        T *nxt = buf + (((last - i) & 1) ^ 1) * 3 * nn;
-        load_rhs(sr, g.d, i, n, g.k, g.j0, kc);
+        const int cb = (int)((last - i) & 1);
+        T *cur = buf + cb * 3 * nn;
+        T *nxt = buf + (cb ^ 1) * 3 * nn;
+        T *sr = srb + cb * nkc;
         cp_async_wait_all();
         __syncthreads();
         if (i > first) {
             async_copy(nxt, g.Af + (i - 1) * (long long)nn, nn);
             async_copy(nxt + nn, g.Bf + (i - 1) * (long long)nn, nn);
+            async_copy(srb + (cb ^ 1) * nkc, rhs_ptr<T>(g.d, i - 1, n, g.k, g.j0), nkc);
         }
         cp_async_commit();
         if (i < last) {
@@ -837,12 +940,13 @@ __global__ void __launch_bounds__(SOLVE_THREADS) chain_bwd_kernel(SolveArgs<T> g
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = g.n, kc = g.kc;
     const int nn = n * n;
+    const int nkc = n * kc;
     T *buf = reinterpret_cast<T *>(smem_raw);  // [2][3][nn]: V_i, W_i, Y_i
-    T *sz = buf + 6 * nn;
-    T *sxL = sz + n * kc;
-    T *sxn = sxL + n * kc;
-    T *sxt = sxn + n * kc;
-    T *red = sxt + 2 * n * kc;
+    T *szb = buf + 6 * nn;                     // [2][nkc]: y_i of the step (prefetched)
+    T *sxL = szb + 2 * nkc;
+    T *sxn = sxL + nkc;
+    T *sxt = sxn + nkc;
+    T *red = sxt + nkc;
     const long long p = blockIdx.x;
     const long long sL = (p * (g.N - 1)) / g.Q;
     const long long sR = ((p + 1) * (g.N - 1)) / g.Q;
@@ -851,6 +955,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS) chain_bwd_kernel(SolveArgs<T> g
     async_copy(buf, g.Af + last * (long long)nn, nn);
     async_copy(buf + nn, g.Bf + last * (long long)nn, nn);
     async_copy(buf + 2 * nn, g.Y + last * (long long)nn, nn);
+    async_copy(szb, rhs_ptr<T>(g.d, last, n, g.k, g.j0), nkc);
     cp_async_commit();
     load_rhs(sxL, xs, p, n, g.k, g.j0, kc);
     load_rhs(sxn, xs, p + 1, n, g.k, g.j0, kc);
@@ -858,15 +963,17 @@ __global__ void __launch_bounds__(SOLVE_THREADS) chain_bwd_kernel(SolveArgs<T> g
     store_rhs(g.d, sxL, sL, n, g.k, g.j0, kc);
     if (p == g.Q - 1) store_rhs(g.d, sxn, sR, n, g.k, g.j0, kc);
     for (long long i = last; i >= first; --i) {
-        T *cur = buf + ((last - i) & 1) * 3 * nn;
-        T *nxt = buf + (((last - i) & 1) ^ 1) * 3 * nn;
-        load_rhs(sz, g.d, i, n, g.k, g.j0, kc);
+        const int cb = (int)((last - i) & 1);
+        T *cur = buf + cb * 3 * nn;
+        T *nxt = buf + (cb ^ 1) * 3 * nn;
+        T *sz = szb + cb * nkc;
         cp_async_wait_all();
         __syncthreads();
         if (i > first) {
             async_copy(nxt, g.Af + (i - 1) * (long long)nn, nn);
             async_copy(nxt + nn, g.Bf + (i - 1) * (long long)nn, nn);
             async_copy(nxt + 2 * nn, g.Y + (i - 1) * (long long)nn, nn);
+            async_copy(szb + (cb ^ 1) * nkc, rhs_ptr<T>(g.d, i - 1, n, g.k, g.j0), nkc);
         }
         cp_async_commit();
         cta_nmul<T>(cur + 2 * nn, sxL, cur + nn, sxn, sz, sz, T(-1), n, kc, red);
@@ -917,53 +1024,211 @@ __global__ void absmax_kernel(const T *__restrict__ v, long long count, unsigned
     if ((threadIdx.x & 31) == 0) atomic_max_nonneg(dst, best);
 }
 
-// r = d - T x in FP64 for one block per CTA; writes r (as Tr) and folds
-// max|r| and max|x| into the status.
+// r = d - T x in FP64 over the block-tridiagonal operator.  The FP64 FMA
+// pipe (~2 per clock per SM on GB300) bounds this kernel, not HBM, so it is
+// shaped to keep that pipe fed: several small CTAs per SM, each owning a
+// contiguous range of blocks.  For block i a thread (row r, column part p)
+// reads A_i(r, c) and B_i(r, c) straight from global memory (coalesced along
+// r) for t_i = A_i x_i + B_i x_{i+1}, and drops B_i into shared memory
+// (ld n+1) for u_{i+1} = B_i^T x_i, the next block's sub-diagonal term; every
+// A and B block is read from HBM once.  Writes r (as Tr; may be null) and
+// folds max|r|, max|x| -- and, when with_norm, the row sums of |T|
+// (||T||_inf) -- into the status.  Columns j0 .. j0+k-1 per launch.
+constexpr int RES_THREADS = 256;
+
+template <class T>
+__host__ __device__ constexpr size_t residual_smem_bytes(int n, int k)
+{
+    // sB (n(n+1)), x ring [3][nk], u ping-pong [2][nk], partials [2][parts<=8][nk],
+    // norm partials [3][8][n] and the carried |B^T| row sums [2][n]
+    return (size_t)(n * (n + 1) + 3 * n * k + 2 * n * k + 16 * n * k + 26 * n) * sizeof(double);
+}
+
+// |x| of an FP64 value as an approximate FP32 (truncated mantissa, 2^-20
+// relative), using integer operations only: on GB300 every warp-instruction
+// on the FP64 pipe costs ~16 cycles, which the operator-norm sums must not add
+__device__ __forceinline__ float abs_f32_approx(double v)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+    if (e <= 0) return 0.0f;
+    if (e >= 255) return __int_as_float(0x7F800000);
+    return __int_as_float((e << 23) | (int)((b >> 29) & 0x7FFFFF));
+}
+__device__ __forceinline__ float abs_f32_approx(float v) { return fabsf(v); }
+
+// one pass of RHS columns jb .. jb+KB-1 over this thread's column range
+template <int KB, class T>
+__device__ __forceinline__ void residual_rows(const T *__restrict__ Ag, const T *__restrict__ Bg, bool has_b, int c0,
+                                              int c1, int n, int LDp, const double *x0, const double *x1, double *sB,
+                                              bool stage_b, double *out, int stride)
+{
+    double acc[KB];
+#pragma unroll
+    for (int q = 0; q < KB; ++q) acc[q] = 0.0;
+    if (has_b) {
+#pragma unroll 4
+        for (int c = c0; c < c1; ++c) {
+            const double a = (double)Ag[(long long)c * n];
+            const double b = (double)Bg[(long long)c * n];
+            if (stage_b) sB[c * LDp] = b;
+#pragma unroll
+            for (int q = 0; q < KB; ++q) acc[q] = fma(a, x0[c + q * n], fma(b, x1[c + q * n], acc[q]));
+        }
+    } else {
+#pragma unroll 4
+        for (int c = c0; c < c1; ++c) {
+            const double a = (double)Ag[(long long)c * n];
+#pragma unroll
+            for (int q = 0; q < KB; ++q) acc[q] = fma(a, x0[c + q * n], acc[q]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < KB; ++q) out[q * stride] = acc[q];
+}
+
 template <class T, class Tr>
-__global__ void residual_kernel(const T *__restrict__ A, const T *__restrict__ B, const T *__restrict__ x,
-                                const T *__restrict__ d, Tr *__restrict__ r, long long N, int n, int k,
-                                DevStatus *st)
+__global__ void __launch_bounds__(RES_THREADS, 3) residual_kernel(const T *__restrict__ A, const T *__restrict__ B,
+                                                               const T *__restrict__ x, const T *__restrict__ d,
+                                                               Tr *__restrict__ r, long long N, int n, int ktot,
+                                                               int j0, int k, long long per_cta, int with_norm,
+                                                               DevStatus *st)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double *sBt = reinterpret_cast<double *>(smem_raw);  // B_{i-1}, ld n+1
-    double *sx = sBt + n * (n + 1);                       // x_{i-1}, x_i, x_{i+1}: 3 * n * k
-    const long long i = blockIdx.x;
+    const int LDp = n + 1;
+    const int nk = n * k;
+    const long long bstride = (long long)n * ktot, coff = (long long)j0 * n;
+    double *sB = reinterpret_cast<double *>(smem_raw);
+    double *sxr = sB + n * LDp;     // [3][nk]
+    double *sub = sxr + 3 * nk;     // [2][nk] u_i ping-pong
+    double *red = sub + 2 * nk;     // [2][8][nk]
+    double *rowred = red + 16 * nk; // [3][8][n]
+    double *rowu = rowred + 24 * n; // [2][n]
+    int parts = RES_THREADS / n;
+    parts = parts < 1 ? 1 : (parts > 8 ? 8 : parts);
+    const int tid = threadIdx.x;
+    const int row = tid % n, part = tid / n;
+    const bool active = part < parts;
+    const int c0 = active ? (part * n) / parts : 0, c1 = active ? ((part + 1) * n) / parts : 0;
     const long long nn = (long long)n * n;
-    const long long nk = (long long)n * k;
-    for (int e = threadIdx.x; e < 3 * n * k; e += blockDim.x) {
-        const int q = e / (n * k), w = e % (n * k);
-        const long long blk = i - 1 + q;
-        sx[e] = (blk >= 0 && blk < N) ? (double)x[blk * nk + w] : 0.0;
+    const long long b0 = (long long)blockIdx.x * per_cta;
+    const long long b1 = (b0 + per_cta < N) ? b0 + per_cta : N;
+    if (b0 >= N) return;
+    double rmax = 0.0, xmax = 0.0, amax = 0.0;
+    auto xs = [&](long long blk) { return sxr + (int)((blk - b0 + 3) % 3) * nk; };  // blk in [b0-1, b1]
+
+    // prologue: x_{b0-1}, x_{b0}, x_{b0+1}; u_{b0} = B_{b0-1}^T x_{b0-1}
+    for (int e = tid; e < nk; e += blockDim.x) {
+        xs(b0)[e] = (double)x[b0 * bstride + coff + e];
+        if (b0 + 1 < N) xs(b0 + 1)[e] = (double)x[(b0 + 1) * bstride + coff + e];
+        sub[e] = 0.0;
     }
-    if (i >= 1)
-        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-            const int rr = e % n, cc = e / n;
-            sBt[rr + cc * (n + 1)] = (double)B[(i - 1) * nn + e];
+    for (int e = tid; e < n; e += blockDim.x) rowu[e] = 0.0;
+    if (b0 > 0) {
+        double *xm = xs(b0 - 1);
+        for (int e = tid; e < nk; e += blockDim.x) xm[e] = (double)x[(b0 - 1) * bstride + coff + e];
+        for (int e = tid; e < (int)nn; e += blockDim.x) {
+            const int c = e / n, rr = e - c * n;
+            sB[rr + c * LDp] = (double)B[(b0 - 1) * nn + e];
         }
+        __syncthreads();
+        for (int o = tid; o < nk; o += blockDim.x) {
+            const int j = o / n, rr = o - j * n;
+            double s = 0.0;
+            for (int c = 0; c < n; ++c) s = fma(sB[c + rr * LDp], xm[c + j * n], s);
+            sub[o] = s;
+        }
+        if (with_norm)
+            for (int rr = tid; rr < n; rr += blockDim.x) {
+                double s = 0.0;
+                for (int c = 0; c < n; ++c) s += fabs(sB[c + rr * LDp]);
+                rowu[rr] = s;
+            }
+    }
     __syncthreads();
-    double rmax = 0.0, xmax = 0.0;
-    for (int o = threadIdx.x; o < n * k; o += blockDim.x) {
-        const int row = o % n, j = o / n;
-        double s = (double)d[i * nk + o];
-        const double *xm = sx + j * n;
-        const double *x0 = sx + n * k + j * n;
-        const double *xp = sx + 2 * n * k + j * n;
-        for (int c = 0; c < n; ++c) s = fma(-(double)A[i * nn + row + (long long)c * n], x0[c], s);
-        if (i + 1 < N)
-            for (int c = 0; c < n; ++c) s = fma(-(double)B[i * nn + row + (long long)c * n], xp[c], s);
-        if (i >= 1)
-            for (int c = 0; c < n; ++c) s = fma(-sBt[c + row * (n + 1)], xm[c], s);
-        if (r) r[i * nk + o] = (Tr)s;
-        rmax = fmax(rmax, fabs(s));
-        xmax = fmax(xmax, fabs(x0[row]));
+
+    for (long long i = b0; i < b1; ++i) {
+        const int par = (int)((i - b0) & 1);
+        const bool has_b = i + 1 < N;
+        const double *x0 = xs(i);
+        const double *x1 = xs(i + 1);
+        double *su = sub + par * nk;        // u_i
+        double *sun = sub + (par ^ 1) * nk;  // u_{i+1}
+        double *rw = rowu + par * 0;         // carried row sums (same slot, owner-updated)
+        // phase 1: t partials from global A_i, B_i; B_i into shared memory
+        if (active) {
+            const T *Ag = A + i * nn + row;
+            const T *Bg = B + i * nn + row;
+            // right-hand sides in compile-time groups (4, then 1): no predicated FP64 FMAs
+            int jb = 0;
+            for (; jb + 4 <= k; jb += 4)
+                residual_rows<4, T>(Ag, Bg, has_b, c0, c1, n, LDp, x0 + jb * n, x1 + jb * n, sB + row, jb == 0,
+                                    red + (part * k + jb) * n + row, n);
+            for (; jb < k; ++jb)
+                residual_rows<1, T>(Ag, Bg, has_b, c0, c1, n, LDp, x0 + jb * n, x1 + jb * n, sB + row, jb == 0,
+                                    red + (part * k + jb) * n + row, n);
+            if (!has_b)
+                for (int c = c0; c < c1; ++c) sB[row + c * LDp] = 0.0;
+            if (with_norm) {
+                float sa = 0.0f;
+                for (int c = c0; c < c1; ++c)
+                    sa += abs_f32_approx(Ag[(long long)c * n]) + (has_b ? abs_f32_approx(Bg[(long long)c * n]) : 0.0f);
+                rowred[part * n + row] = sa;
+            }
+        }
+        __syncthreads();
+        // phase 2: u_{i+1} partials from the staged B_i
+        if (active && has_b) {
+            for (int j = 0; j < k; ++j) {
+                double u = 0.0;
+                for (int c = c0; c < c1; ++c) u = fma(sB[c + row * LDp], x0[c + j * n], u);
+                red[8 * nk + (part * k + j) * n + row] = u;
+            }
+            if (with_norm) {
+                float sbt = 0.0f;
+                for (int c = c0; c < c1; ++c) sbt += abs_f32_approx(sB[c + row * LDp]);
+                rowred[16 * n + part * n + row] = sbt;
+            }
+        }
+        __syncthreads();
+        // phase 3: outputs; fetch x_{i+2}
+        for (int o = tid; o < nk; o += blockDim.x) {
+            const int j = o / n, rr = o - j * n;
+            double t = 0.0, u = 0.0;
+            for (int q = 0; q < parts; ++q) t += red[(q * k + j) * n + rr];
+            if (has_b)
+                for (int q = 0; q < parts; ++q) u += red[8 * nk + (q * k + j) * n + rr];
+            const double res = (double)d[i * bstride + coff + o] - t - su[o];
+            if (r) r[i * bstride + coff + o] = (Tr)res;
+            rmax = fmax(rmax, fabs(res));
+            xmax = fmax(xmax, fabs(x0[o]));
+            sun[o] = u;
+        }
+        if (with_norm)
+            for (int rr = tid; rr < n; rr += blockDim.x) {
+                double s = rw[rr], s2 = 0.0;
+                for (int q = 0; q < parts; ++q) {
+                    s += rowred[q * n + rr];
+                    if (has_b) s2 += rowred[16 * n + q * n + rr];
+                }
+                amax = fmax(amax, s);
+                rw[rr] = has_b ? s2 : 0.0;
+            }
+        if (i + 2 < N && i + 1 < b1) {
+            double *x2 = xs(i + 2);
+            for (int e = tid; e < nk; e += blockDim.x) x2[e] = (double)x[(i + 2) * bstride + coff + e];
+        }
+        __syncthreads();
     }
     for (int o = 16; o > 0; o >>= 1) {
         rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
         xmax = fmax(xmax, __shfl_xor_sync(0xffffffffu, xmax, o));
+        amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
     }
     if ((threadIdx.x & 31) == 0) {
         atomic_max_nonneg(&st->rnorm, rmax);
         atomic_max_nonneg(&st->xnorm, xmax);
+        if (with_norm) atomic_max_nonneg(&st->anorm, amax);
     }
 }
 

@@ -38,7 +38,7 @@ template <class T>
 cudaError_t launch_absmax(const T *v, long long count, unsigned long long *dst, cudaStream_t s);
 template <class T, class Tr>
 cudaError_t launch_residual(const T *A, const T *B, const T *x, const T *d, Tr *r, long long N, int n, int k,
-                            DevStatus *st, cudaStream_t s);
+                            int with_norm, DevStatus *st, cudaStream_t s);
 cudaError_t launch_relres(DevStatus *st, double tol, cudaStream_t s);
 template <class Tc>
 cudaError_t launch_update(double *x, const Tc *c, long long count, int assign, cudaStream_t s);

@@ -128,16 +128,31 @@ cudaError_t launch_absmax(const T *v, long long count, unsigned long long *dst, 
 
 template <class T, class Tr>
 cudaError_t launch_residual(const T *A, const T *B, const T *x, const T *d, Tr *r, long long N, int n, int k,
-                            DevStatus *st, cudaStream_t s)
+                            int with_norm, DevStatus *st, cudaStream_t s)
 {
-    const size_t smem = (size_t)(n * (n + 1) + 3 * n * k) * sizeof(double);
     auto kern = residual_kernel<T, Tr>;
+    int kc = k;
+    while (kc > 1 && residual_smem_bytes<T>(n, kc) > (size_t)200 * 1024) kc = (kc + 1) / 2;
+    const size_t smem = residual_smem_bytes<T>(n, kc);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    int threads = n * k < 256 ? ((n * k + 31) / 32) * 32 : 256;
-    kern<<<(unsigned)N, threads, smem, s>>>(A, B, x, d, r, N, n, k, st);
-    count_launch();
-    return cudaGetLastError();
+    int dev = 0, sms = 1, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, RES_THREADS, smem);
+    long long grid = (long long)sms * (per_sm > 0 ? per_sm : 1);
+    if (grid > N) grid = N;
+    const long long per_cta = (N + grid - 1) / grid;
+    grid = (N + per_cta - 1) / per_cta;
+    for (int j0 = 0; j0 < k; j0 += kc) {
+        const int kk = (k - j0 < kc) ? k - j0 : kc;
+        kern<<<(unsigned)grid, RES_THREADS, smem, s>>>(A, B, x, d, r, N, n, k, j0, kk, per_cta,
+                                                       (with_norm && j0 == 0) ? 1 : 0, st);
+        count_launch();
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 template <class Tc>

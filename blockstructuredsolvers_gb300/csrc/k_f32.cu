@@ -19,7 +19,7 @@ template cudaError_t launch_assemble_rhs<float, double>(const float *, const flo
 template cudaError_t launch_opnorm<float>(const float *, const float *, long long, int, DevStatus *, cudaStream_t);
 template cudaError_t launch_absmax<float>(const float *, long long, unsigned long long *, cudaStream_t);
 template cudaError_t launch_residual<float, float>(const float *, const float *, const float *, const float *,
-                                                   float *, long long, int, int, DevStatus *, cudaStream_t);
+                                                   float *, long long, int, int, int, DevStatus *, cudaStream_t);
 template cudaError_t launch_update<float>(double *, const float *, long long, int, cudaStream_t);
 template cudaError_t launch_convert<float, double>(double *, const float *, long long, cudaStream_t);
 template cudaError_t launch_init_identity<float>(float *, long long, long long, int, cudaStream_t);

@@ -16,7 +16,7 @@ template cudaError_t launch_opnorm<double>(const double *, const double *, long 
                                            cudaStream_t);
 template cudaError_t launch_absmax<double>(const double *, long long, unsigned long long *, cudaStream_t);
 template cudaError_t launch_residual<double, double>(const double *, const double *, const double *,
-                                                     const double *, double *, long long, int, int, DevStatus *,
+                                                     const double *, double *, long long, int, int, int, DevStatus *,
                                                      cudaStream_t);
 template cudaError_t launch_update<double>(double *, const double *, long long, int, cudaStream_t);
 template cudaError_t launch_init_identity<double>(double *, long long, long long, int, cudaStream_t);

@@ -13,7 +13,7 @@ template cudaError_t launch_assemble_schur<double, float, double>(const double *
                                                                   double *, long long, long long, int,
                                                                   cudaStream_t);
 template cudaError_t launch_residual<double, float>(const double *, const double *, const double *,
-                                                    const double *, float *, long long, int, int, DevStatus *,
+                                                    const double *, float *, long long, int, int, int, DevStatus *,
                                                     cudaStream_t);
 template cudaError_t launch_convert<double, float>(float *, const double *, long long, cudaStream_t);
 template cudaError_t launch_convert<double, double>(double *, const double *, long long, cudaStream_t);

@@ -134,7 +134,9 @@ int bss_plan_reference(int64_t N, int64_t *levels, int32_t maxlev, int32_t *nlev
 
 /* Relative residual ||d - T x||_inf / (||T||_inf ||x||_inf + ||d||_inf) of a
  * block-tridiagonal system held in caller device buffers (same layouts),
- * computed on the device in FP64.  Blocks on `stream`; result in *out. */
+ * computed on the device: d - T x in FP64; ||T||_inf accumulated in FP32
+ * from FP64 magnitudes (relative accuracy ~1e-6, which only scales the
+ * ratio).  Blocks on `stream`; result in *out. */
 int bss_residual(int64_t N, int64_t n, int64_t k, int32_t dtype, const void *A, const void *B,
                  const void *x, const void *d, void *stream, double *out);
 

@@ -251,7 +251,8 @@ def test_residual_entry_point(bss):
     dt.copy_(to(d))
     r = bss.residual(At, Bt, xt, dt)
     want = O.rel_residual(A, B, x, d)
-    assert want > 1e-9 and abs(r - want) <= 1e-9 * want
+    # numerator in FP64; ||T||_inf accumulated in FP32 (relative accuracy ~1e-6)
+    assert want > 1e-9 and abs(r - want) <= 1e-5 * want
 
 
 @pytest.mark.parametrize("T", ["f64", "f32", "mixed"])
