@@ -92,6 +92,19 @@ struct bss_handle {
     int kc_max = 1;
     bss_info info{};
     int sticky = BSS_OK;
+    // CUDA graphs: the first call of each kind runs eagerly on `stream`; later
+    // calls replay a graph captured on cap_stream and launched on `stream`
+    cudaStream_t ls = nullptr;          // stream the launch code enqueues on
+    cudaStream_t cap_stream = nullptr;  // private capture streams
+    cudaStream_t cap_stream2 = nullptr;
+    cudaGraphExec_t g_factor = nullptr, g_solve = nullptr;
+    int n_factor = 0, n_solve = 0;
+    // kernels per replay (captured launches); mixed solve: prologue, loop
+    // body (residual + decision) and correction, combined at synchronize
+    long long k_factor = 0, k_solve = 0, k_pro = 0, k_body = 0, k_corr = 0;
+    long long graph_solves_unsynced = 0;        // device-loop solves launched since the last sync
+    unsigned long long iters_total_seen = 0;    // st->iters_total at the last sync
+    bool graph_solve_pending = false;   // a graph solve ran: read its outcome at synchronize
 };
 
 extern "C" void bss_default_options(bss_options *o)
@@ -390,6 +403,7 @@ int create_common(bss_handle *h, int64_t N, int64_t n, int64_t k, int32_t dtype,
     h->k = k;
     h->dtype = dtype;
     h->stream = (cudaStream_t)stream;
+    h->ls = h->stream;
     cudaError_t e = cudaGetDevice(&h->device);
     if (e != cudaSuccess) {
         delete h;
@@ -452,6 +466,10 @@ extern "C" int bss_destroy(bss_handle *h)
     if (!h) return BSS_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
     else cudaDeviceSynchronize();
+    if (h->g_factor) cudaGraphExecDestroy(h->g_factor);
+    if (h->g_solve) cudaGraphExecDestroy(h->g_solve);
+    if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+    if (h->cap_stream2) cudaStreamDestroy(h->cap_stream2);
     if (h->arena) cudaFree(h->arena);
     if (h->h_st) cudaFreeHost(h->h_st);
     delete h;
@@ -499,7 +517,7 @@ cudaError_t factor_level(bss_handle *h, int l)
     a.seq = L.seq ? 1 : 0;
     a.level = l;
     a.st = h->st;
-    return launch_chain_factor<Tin, T>(a, h->stream);
+    return launch_chain_factor<Tin, T>(a, h->ls);
 }
 
 cudaError_t assemble_level(bss_handle *h, int l)
@@ -509,19 +527,19 @@ cudaError_t assemble_level(bss_handle *h, int l)
     const int n = (int)h->n;
     if (L.tin == F64 && L.t == F64)
         return launch_assemble_schur<double, double, double>((const double *)L.A, (const double *)L.C,
-                                                             (double *)X.A, (double *)X.B, L.N, L.Q, n, h->stream);
+                                                             (double *)X.A, (double *)X.B, L.N, L.Q, n, h->ls);
     if (L.tin == F32 && L.t == F32 && X.t == F32)
         return launch_assemble_schur<float, float, float>((const float *)L.A, (const float *)L.C, (float *)X.A,
-                                                          (float *)X.B, L.N, L.Q, n, h->stream);
+                                                          (float *)X.B, L.N, L.Q, n, h->ls);
     if (L.tin == F32 && L.t == F32 && X.t == F64)
         return launch_assemble_schur<float, float, double>((const float *)L.A, (const float *)L.C, (double *)X.A,
-                                                           (double *)X.B, L.N, L.Q, n, h->stream);
+                                                           (double *)X.B, L.N, L.Q, n, h->ls);
     if (L.tin == F64 && L.t == F32 && X.t == F32)
         return launch_assemble_schur<double, float, float>((const double *)L.A, (const float *)L.C, (float *)X.A,
-                                                           (float *)X.B, L.N, L.Q, n, h->stream);
+                                                           (float *)X.B, L.N, L.Q, n, h->ls);
     if (L.tin == F64 && L.t == F32 && X.t == F64)
         return launch_assemble_schur<double, float, double>((const double *)L.A, (const float *)L.C,
-                                                            (double *)X.A, (double *)X.B, L.N, L.Q, n, h->stream);
+                                                            (double *)X.A, (double *)X.B, L.N, L.Q, n, h->ls);
     return cudaErrorInvalidValue;
 }
 
@@ -538,11 +556,13 @@ cudaError_t factor_any(bss_handle *h, int l)
 
 static int factorize_upto(bss_handle *h, int upto)
 {
-    BSS_CUDA(cudaMemsetAsync(&h->st->bad_key, 0xFF, sizeof(unsigned long long), h->stream));
+    BSS_CUDA(cudaMemsetAsync(&h->st->bad_key, 0xFF, sizeof(unsigned long long), h->ls));
     const bool mixed = h->opt.precision == BSS_PRECISION_MIXED;
     if (mixed) {
         // ||T||_inf is folded into the first residual after this factorization
-        BSS_CUDA(cudaMemsetAsync(&h->st->anorm, 0, sizeof(unsigned long long), h->stream));
+        BSS_CUDA(cudaMemsetAsync(&h->st->anorm, 0, sizeof(unsigned long long), h->ls));
+        BSS_CUDA(cudaMemsetAsync(&h->st->need_anorm, 0, sizeof(int), h->ls));
+        BSS_CUDA(cudaMemsetAsync(&h->st->need_anorm, 1, 1, h->ls));
         h->need_anorm = true;
     }
     const int nlev = (int)h->levels.size();
@@ -555,15 +575,58 @@ static int factorize_upto(bss_handle *h, int upto)
     return BSS_OK;
 }
 
+// Run `body` (which enqueues on h->ls): eagerly on the first call, afterwards
+// as a CUDA graph captured once on a private stream and launched on the
+// handle's stream (the caller's stream may be the legacy default stream,
+// which cannot be captured).
+template <class F>
+static int run_graphed(bss_handle *h, cudaGraphExec_t &exec, int &ncalls, long long &nkern, F body)
+{
+    if (!h->opt.use_graphs || ncalls++ == 0) {
+        h->ls = h->stream;
+        return body();
+    }
+    if (!exec) {
+        const long long k0 = launch_count();
+        if (!h->cap_stream) BSS_CUDA(cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking));
+        if (!h->cap_stream2) BSS_CUDA(cudaStreamCreateWithFlags(&h->cap_stream2, cudaStreamNonBlocking));
+        h->ls = h->cap_stream;
+        BSS_CUDA(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeRelaxed));
+        const int rc = body();
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(h->cap_stream, &g);
+        h->ls = h->stream;
+        if (rc != BSS_OK || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return rc != BSS_OK ? rc : cuda_fail(e, "cudaStreamEndCapture");
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            exec = nullptr;
+            return cuda_fail(ei, "cudaGraphInstantiate");
+        }
+        nkern = launch_count() - k0;
+        count_launches(-nkern);  // capture launched nothing; replays are counted below
+    }
+    BSS_CUDA(cudaGraphLaunch(exec, h->stream));
+    if (nkern >= 0) count_launches(nkern);
+    return BSS_OK;
+}
+
 extern "C" int bss_factorize(bss_handle *h)
 {
     if (!h) return fail(BSS_ERR_ARG, "handle is NULL");
-    return factorize_upto(h, (int)h->levels.size());
+    const int nlev = (int)h->levels.size();
+    const int rc = run_graphed(h, h->g_factor, h->n_factor, h->k_factor, [&]() { return factorize_upto(h, nlev); });
+    h->factored = true;
+    return rc;
 }
 
 extern "C" int bss_factorize_levels(bss_handle *h, int32_t nlevels)
 {
     if (!h) return fail(BSS_ERR_ARG, "handle is NULL");
+    h->ls = h->stream;
     if (nlevels < 0 || nlevels >= (int)h->levels.size())
         return fail(BSS_ERR_ARG, "nlevels must be in [0, number of partitioned levels]");
     return factorize_upto(h, nlevels);
@@ -613,8 +676,8 @@ SolveArgs<T> solve_args(bss_handle *h, int l, int j0, int kc)
 cudaError_t fwd_level(bss_handle *h, int l, int j0, int kc)
 {
     const Level &L = h->levels[l];
-    if (L.t == F64) return launch_chain_fwd<double>(solve_args<double>(h, l, j0, kc), h->stream);
-    return launch_chain_fwd<float>(solve_args<float>(h, l, j0, kc), h->stream);
+    if (L.t == F64) return launch_chain_fwd<double>(solve_args<double>(h, l, j0, kc), h->ls);
+    return launch_chain_fwd<float>(solve_args<float>(h, l, j0, kc), h->ls);
 }
 
 cudaError_t rhs_level(bss_handle *h, int l, int j0, int kc)
@@ -624,13 +687,13 @@ cudaError_t rhs_level(bss_handle *h, int l, int j0, int kc)
     const int n = (int)h->n, k = (int)h->k;
     if (L.t == F64 && X.t == F64)
         return launch_assemble_rhs<double, double>((const double *)L.d, (const double *)L.bvec, (double *)X.d, L.N,
-                                                   L.Q, n, k, j0, kc, h->stream);
+                                                   L.Q, n, k, j0, kc, h->ls);
     if (L.t == F32 && X.t == F32)
         return launch_assemble_rhs<float, float>((const float *)L.d, (const float *)L.bvec, (float *)X.d, L.N, L.Q,
-                                                 n, k, j0, kc, h->stream);
+                                                 n, k, j0, kc, h->ls);
     if (L.t == F32 && X.t == F64)
         return launch_assemble_rhs<float, double>((const float *)L.d, (const float *)L.bvec, (double *)X.d, L.N,
-                                                  L.Q, n, k, j0, kc, h->stream);
+                                                  L.Q, n, k, j0, kc, h->ls);
     return cudaErrorInvalidValue;
 }
 
@@ -638,9 +701,9 @@ cudaError_t bwd_level(bss_handle *h, int l, int j0, int kc)
 {
     const Level &L = h->levels[l];
     const Level &X = h->levels[l + 1];
-    if (L.t == F64 && X.t == F64) return launch_chain_bwd<double, double>(solve_args<double>(h, l, j0, kc), h->stream);
-    if (L.t == F32 && X.t == F32) return launch_chain_bwd<float, float>(solve_args<float>(h, l, j0, kc), h->stream);
-    if (L.t == F32 && X.t == F64) return launch_chain_bwd<float, double>(solve_args<float>(h, l, j0, kc), h->stream);
+    if (L.t == F64 && X.t == F64) return launch_chain_bwd<double, double>(solve_args<double>(h, l, j0, kc), h->ls);
+    if (L.t == F32 && X.t == F32) return launch_chain_bwd<float, float>(solve_args<float>(h, l, j0, kc), h->ls);
+    if (L.t == F32 && X.t == F64) return launch_chain_bwd<float, double>(solve_args<float>(h, l, j0, kc), h->ls);
     return cudaErrorInvalidValue;
 }
 
@@ -666,35 +729,36 @@ int solve_mixed(bss_handle *h)
     const double *d64 = (const double *)h->d;
     const bool c_is_f32 = h->levels[0].t == F32;
     DevStatus *st = h->st;
-    BSS_CUDA(cudaMemsetAsync(&st->dnorm, 0, sizeof(unsigned long long), h->stream));
-    BSS_CUDA(launch_absmax<double>(d64, cnt, &st->dnorm, h->stream));
+    BSS_CUDA(cudaMemsetAsync(&st->dnorm, 0, sizeof(unsigned long long), h->ls));
+    BSS_CUDA(launch_absmax<double>(d64, cnt, &st->dnorm, h->ls));
     if (c_is_f32)
-        BSS_CUDA((launch_convert<double, float>((float *)h->c0, d64, cnt, h->stream)));
+        BSS_CUDA((launch_convert<double, float>((float *)h->c0, d64, cnt, h->ls)));
     else
-        BSS_CUDA((launch_convert<double, double>((double *)h->c0, d64, cnt, h->stream)));
+        BSS_CUDA((launch_convert<double, double>((double *)h->c0, d64, cnt, h->ls)));
     int rc = chain_solve(h);
     if (rc) return rc;
     if (c_is_f32)
-        BSS_CUDA(launch_update<float>(h->x64, (const float *)h->c0, cnt, 1, h->stream));
+        BSS_CUDA(launch_update<float>(h->x64, (const float *)h->c0, cnt, 1, h->ls));
     else
-        BSS_CUDA(launch_update<double>(h->x64, (const double *)h->c0, cnt, 1, h->stream));
+        BSS_CUDA(launch_update<double>(h->x64, (const double *)h->c0, cnt, 1, h->ls));
     int steps = 0;
     bool converged = false;
     for (int it = 0; it <= h->opt.max_refine; ++it) {
-        BSS_CUDA(cudaMemsetAsync(&st->rnorm, 0, 2 * sizeof(unsigned long long), h->stream));
+        BSS_CUDA(cudaMemsetAsync(&st->rnorm, 0, 2 * sizeof(unsigned long long), h->ls));
         const int wn = h->need_anorm ? 1 : 0;
         h->need_anorm = false;
+        if (wn) BSS_CUDA(cudaMemsetAsync(&st->need_anorm, 0, sizeof(int), h->ls));
         if (c_is_f32)
             BSS_CUDA((launch_residual<double, float>((const double *)h->A, (const double *)h->B, h->x64, d64,
                                                      (float *)h->c0, h->N, (int)h->n, (int)h->k, wn, st,
-                                                     h->stream)));
+                                                     h->ls)));
         else
             BSS_CUDA((launch_residual<double, double>((const double *)h->A, (const double *)h->B, h->x64, d64,
                                                       (double *)h->c0, h->N, (int)h->n, (int)h->k, wn, st,
-                                                      h->stream)));
-        BSS_CUDA(launch_relres(st, h->opt.tol, h->stream));
-        BSS_CUDA(cudaMemcpyAsync(h->h_st, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->stream));
-        BSS_CUDA(cudaStreamSynchronize(h->stream));
+                                                      h->ls)));
+        BSS_CUDA(launch_relres(st, h->opt.tol, h->ls));
+        BSS_CUDA(cudaMemcpyAsync(h->h_st, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->ls));
+        BSS_CUDA(cudaStreamSynchronize(h->ls));
         h->info.rel_residual = h->h_st->relres;
         if (h->h_st->done) {
             converged = true;
@@ -704,14 +768,110 @@ int solve_mixed(bss_handle *h)
         rc = chain_solve(h);
         if (rc) return rc;
         if (c_is_f32)
-            BSS_CUDA(launch_update<float>(h->x64, (const float *)h->c0, cnt, 0, h->stream));
+            BSS_CUDA(launch_update<float>(h->x64, (const float *)h->c0, cnt, 0, h->ls));
         else
-            BSS_CUDA(launch_update<double>(h->x64, (const double *)h->c0, cnt, 0, h->stream));
+            BSS_CUDA(launch_update<double>(h->x64, (const double *)h->c0, cnt, 0, h->ls));
         ++steps;
     }
     h->info.refine_steps = steps;
-    BSS_CUDA(cudaMemcpyAsync(h->d, h->x64, cnt * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    BSS_CUDA(cudaMemcpyAsync(h->d, h->x64, cnt * sizeof(double), cudaMemcpyDeviceToDevice, h->ls));
     if (!converged) h->sticky = BSS_ERR_NOT_CONVERGED;
+    return BSS_OK;
+}
+
+// Mixed solve as one graph with the refinement loop on the device:
+//   prologue (x = first FP32-factor solve)
+//   WHILE(loop) { residual (FP64); decide on the device (relres_control);
+//                 IF(correct) { FP32-factor solve of r; x += c } }
+//   copy x -> d
+// relres_control sets both conditional values; the host reads the outcome
+// (steps, residual, convergence) at bss_synchronize.  Enqueues on h->ls,
+// which is the capture stream cap_stream.
+int capture_mixed_solve(bss_handle *h)
+{
+    const long long cnt = h->N * h->n * h->k;
+    const double *d64 = (const double *)h->d;
+    const bool c_is_f32 = h->levels[0].t == F32;
+    DevStatus *st = h->st;
+    const long long k0 = launch_count();
+    BSS_CUDA(cudaMemsetAsync(&st->dnorm, 0, sizeof(unsigned long long), h->ls));
+    BSS_CUDA(cudaMemsetAsync(&st->iters, 0, sizeof(int), h->ls));
+    BSS_CUDA(cudaMemsetAsync(&st->done, 0, sizeof(int), h->ls));
+    BSS_CUDA(launch_absmax<double>(d64, cnt, &st->dnorm, h->ls));
+    if (c_is_f32)
+        BSS_CUDA((launch_convert<double, float>((float *)h->c0, d64, cnt, h->ls)));
+    else
+        BSS_CUDA((launch_convert<double, double>((double *)h->c0, d64, cnt, h->ls)));
+    int rc = chain_solve(h);
+    if (rc) return rc;
+    if (c_is_f32)
+        BSS_CUDA(launch_update<float>(h->x64, (const float *)h->c0, cnt, 1, h->ls));
+    else
+        BSS_CUDA(launch_update<double>(h->x64, (const double *)h->c0, cnt, 1, h->ls));
+
+    const long long k1 = launch_count();
+    cudaStreamCaptureStatus cst;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    BSS_CUDA(cudaStreamGetCaptureInfo(h->cap_stream, &cst, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphConditionalHandle hloop;
+    BSS_CUDA(cudaGraphConditionalHandleCreate(&hloop, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams wp = {cudaGraphNodeTypeConditional};
+    wp.conditional.handle = hloop;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    BSS_CUDA(cudaGraphAddNode(&wnode, g, deps, nullptr, nd, &wp));
+    cudaGraph_t wbody = wp.conditional.phGraph_out[0];
+    BSS_CUDA(cudaStreamUpdateCaptureDependencies(h->cap_stream, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaGraphConditionalHandle hcorr;
+    BSS_CUDA(cudaGraphConditionalHandleCreate(&hcorr, wbody, 0, cudaGraphCondAssignDefault));
+
+    // loop body: residual + decision, then the conditional correction
+    h->ls = h->cap_stream2;
+    BSS_CUDA(cudaStreamBeginCaptureToGraph(h->cap_stream2, wbody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    BSS_CUDA(cudaMemsetAsync(&st->rnorm, 0, 2 * sizeof(unsigned long long), h->ls));
+    if (c_is_f32)
+        BSS_CUDA((launch_residual<double, float>((const double *)h->A, (const double *)h->B, h->x64, d64,
+                                                 (float *)h->c0, h->N, (int)h->n, (int)h->k, -1, st, h->ls)));
+    else
+        BSS_CUDA((launch_residual<double, double>((const double *)h->A, (const double *)h->B, h->x64, d64,
+                                                  (double *)h->c0, h->N, (int)h->n, (int)h->k, -1, st, h->ls)));
+    BSS_CUDA(launch_relres_control(st, h->opt.tol, h->opt.max_refine, hloop, hcorr, h->ls));
+    const long long k2 = launch_count();
+    cudaGraph_t g2 = nullptr;
+    BSS_CUDA(cudaStreamGetCaptureInfo(h->cap_stream2, &cst, nullptr, &g2, &deps, nullptr, &nd));
+    cudaGraphNodeParams ip = {cudaGraphNodeTypeConditional};
+    ip.conditional.handle = hcorr;
+    ip.conditional.type = cudaGraphCondTypeIf;
+    ip.conditional.size = 1;
+    cudaGraphNode_t inode;
+    BSS_CUDA(cudaGraphAddNode(&inode, g2, deps, nullptr, nd, &ip));
+    cudaGraph_t ibody = ip.conditional.phGraph_out[0];
+    BSS_CUDA(cudaStreamUpdateCaptureDependencies(h->cap_stream2, &inode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaGraph_t wb_out = nullptr;
+    BSS_CUDA(cudaStreamEndCapture(h->cap_stream2, &wb_out));
+    BSS_CUDA(cudaStreamBeginCaptureToGraph(h->cap_stream2, ibody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    rc = chain_solve(h);
+    if (rc == BSS_OK) {
+        if (c_is_f32)
+            rc = launch_update<float>(h->x64, (const float *)h->c0, cnt, 0, h->ls) == cudaSuccess ? BSS_OK : BSS_ERR_CUDA;
+        else
+            rc = launch_update<double>(h->x64, (const double *)h->c0, cnt, 0, h->ls) == cudaSuccess ? BSS_OK
+                                                                                                  : BSS_ERR_CUDA;
+    }
+    const long long k3 = launch_count();
+    h->k_pro = k1 - k0;
+    h->k_body = k2 - k1;
+    h->k_corr = k3 - k2;
+    count_launches(-(k3 - k0));  // capture launched nothing; replays are counted at synchronize
+    cudaGraph_t ib_out = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(h->cap_stream2, &ib_out);
+    h->ls = h->cap_stream;
+    if (rc) return rc;
+    if (e2 != cudaSuccess) return cuda_fail(e2, "capture of the correction body");
+    BSS_CUDA(cudaMemcpyAsync(h->d, h->x64, cnt * sizeof(double), cudaMemcpyDeviceToDevice, h->ls));
     return BSS_OK;
 }
 
@@ -721,8 +881,22 @@ extern "C" int bss_solve(bss_handle *h)
 {
     if (!h) return fail(BSS_ERR_ARG, "handle is NULL");
     if (!h->factored) return fail(BSS_ERR_STATE, "solve before factorize");
-    if (h->opt.precision == BSS_PRECISION_MIXED) return solve_mixed(h);
-    return chain_solve(h);
+    if (h->opt.precision == BSS_PRECISION_MIXED) {
+        if (!h->opt.use_graphs || h->n_solve == 0) {
+            ++h->n_solve;
+            h->ls = h->stream;
+            h->graph_solve_pending = false;
+            return solve_mixed(h);
+        }
+        long long dummy = -1;  // the loop's kernel count is known only at synchronize
+        const int rc = run_graphed(h, h->g_solve, h->n_solve, dummy, [&]() { return capture_mixed_solve(h); });
+        if (rc == BSS_OK) {
+            h->graph_solve_pending = true;
+            ++h->graph_solves_unsynced;
+        }
+        return rc;
+    }
+    return run_graphed(h, h->g_solve, h->n_solve, h->k_solve, [&]() { return chain_solve(h); });
 }
 
 extern "C" int bss_synchronize(bss_handle *h)
@@ -730,6 +904,16 @@ extern "C" int bss_synchronize(bss_handle *h)
     if (!h) return fail(BSS_ERR_ARG, "handle is NULL");
     BSS_CUDA(cudaStreamSynchronize(h->stream));
     BSS_CUDA(cudaMemcpy(h->h_st, h->st, sizeof(DevStatus), cudaMemcpyDeviceToHost));
+    if (h->graph_solve_pending) {  // outcome of the device-side refinement loop
+        h->graph_solve_pending = false;
+        h->info.refine_steps = h->h_st->iters;
+        h->info.rel_residual = h->h_st->relres;
+        const long long dit = (long long)(h->h_st->iters_total - h->iters_total_seen);
+        count_launches(h->graph_solves_unsynced * (h->k_pro + h->k_body) + dit * (h->k_body + h->k_corr));
+        h->graph_solves_unsynced = 0;
+        h->iters_total_seen = h->h_st->iters_total;
+        h->sticky = h->h_st->done ? BSS_OK : BSS_ERR_NOT_CONVERGED;
+    }
     const unsigned long long key = h->h_st->bad_key;
     if (h->factored && key != ~0ULL) {
         h->info.failed_level = (int32_t)(key >> 40);

@@ -52,7 +52,10 @@ struct DevStatus {
     unsigned long long anorm;    // FP64 bits of ||T||_inf
     double relres;
     int done;
+    int iters;        // refinement corrections applied by the last solve
+    int need_anorm;   // the next residual also accumulates ||T||_inf
     int pad;
+    unsigned long long iters_total;  // corrections over all device-loop solves (never reset)
 };
 
 __device__ __forceinline__ void record_bad_pivot(DevStatus *st, int level, long long block)
@@ -1114,6 +1117,7 @@ __global__ void __launch_bounds__(RES_THREADS, 3) residual_kernel(const T *__res
     const long long b0 = (long long)blockIdx.x * per_cta;
     const long long b1 = (b0 + per_cta < N) ? b0 + per_cta : N;
     if (b0 >= N) return;
+    if (with_norm < 0) with_norm = st->need_anorm;  // graph mode: decided on the device
     double rmax = 0.0, xmax = 0.0, amax = 0.0;
     auto xs = [&](long long blk) { return sxr + (int)((blk - b0 + 3) % 3) * nk; };  // blk in [b0-1, b1]
 
@@ -1229,6 +1233,33 @@ __global__ void __launch_bounds__(RES_THREADS, 3) residual_kernel(const T *__res
         atomic_max_nonneg(&st->rnorm, rmax);
         atomic_max_nonneg(&st->xnorm, xmax);
         if (with_norm) atomic_max_nonneg(&st->anorm, amax);
+    }
+}
+
+// one refinement decision on the device (graph mode): relative residual,
+// convergence, and the two conditional-node values (loop again / apply a
+// correction) -- no host round trip per refinement step
+static __global__ void relres_control_kernel(DevStatus *st, double tol, int max_refine,
+                                             cudaGraphConditionalHandle hloop, cudaGraphConditionalHandle hcorr)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const double rn = __longlong_as_double((long long)st->rnorm);
+        const double xn = __longlong_as_double((long long)st->xnorm);
+        const double dn = __longlong_as_double((long long)st->dnorm);
+        const double an = __longlong_as_double((long long)st->anorm);
+        const double den = an * xn + dn;
+        const double rel = den > 0.0 ? rn / den : 0.0;
+        const int done = (rel <= tol) ? 1 : 0;
+        const int cont = (!done && st->iters < max_refine) ? 1 : 0;
+        st->relres = rel;
+        st->done = done;
+        st->need_anorm = 0;
+        if (cont) {
+            st->iters += 1;
+            st->iters_total += 1;
+        }
+        cudaGraphSetConditional(hloop, (unsigned)cont);
+        cudaGraphSetConditional(hcorr, (unsigned)cont);
     }
 }
 

@@ -40,6 +40,8 @@ template <class T, class Tr>
 cudaError_t launch_residual(const T *A, const T *B, const T *x, const T *d, Tr *r, long long N, int n, int k,
                             int with_norm, DevStatus *st, cudaStream_t s);
 cudaError_t launch_relres(DevStatus *st, double tol, cudaStream_t s);
+cudaError_t launch_relres_control(DevStatus *st, double tol, int max_refine, cudaGraphConditionalHandle hloop,
+                                  cudaGraphConditionalHandle hcorr, cudaStream_t s);
 template <class Tc>
 cudaError_t launch_update(double *x, const Tc *c, long long count, int assign, cudaStream_t s);
 template <class Ts, class Td>
@@ -54,6 +56,7 @@ void set_last_error(const std::string &msg);
 
 // process-wide count of kernels this library launched (all handles)
 void count_launch();
+void count_launches(long long n);  // kernels run by a graph replay
 long long launch_count();
 
 }  // namespace bss

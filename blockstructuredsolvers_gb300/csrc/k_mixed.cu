@@ -21,11 +21,20 @@ template cudaError_t launch_convert<float, float>(float *, const float *, long l
 
 static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 cudaError_t launch_relres(DevStatus *st, double tol, cudaStream_t s)
 {
     relres_kernel<<<1, 32, 0, s>>>(st, tol);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_relres_control(DevStatus *st, double tol, int max_refine, cudaGraphConditionalHandle hloop,
+                                  cudaGraphConditionalHandle hcorr, cudaStream_t s)
+{
+    relres_control_kernel<<<1, 32, 0, s>>>(st, tol, max_refine, hloop, hcorr);
     count_launch();
     return cudaGetLastError();
 }

@@ -286,3 +286,28 @@ def test_config1_full_size_properties(bss, T):
     rel = (r.abs().max() / (rs.max() * x.abs().max() + d.abs().max())).item()
     bound = {"f64": 1e-14, "f32": 1e-6, "mixed": 1e-12}[T]
     assert rel <= bound, rel
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_graph_replay_matches_eager(bss, precision):
+    """Calls after the first replay CUDA graphs (the mixed refinement loop on
+    the device); results must equal the eager first call bit for bit and the
+    refinement outcome must be reported after synchronize."""
+    import torch
+    rng = np.random.default_rng(11)
+    A, B, d = O.gen_config0_family(rng, 700, 32, 2)
+    outs = []
+    for use_graphs in (True, False):
+        data = bss.initialize_batched(700, 32, torch.float64, k=2, precision=precision, use_graphs=use_graphs)
+        for rep in range(3):
+            upload(data, A, B, d)
+            bss.factorize_(data)
+            bss.solve_(data)
+            bss.synchronize(data)
+            outs.append(download_x(data, 700))
+            if precision == "mixed":
+                info = bss.get_info(data)
+                assert info["rel_residual"] <= 1e-12 and info["refine_steps"] >= 1
+    for x in outs[1:]:
+        assert np.array_equal(x, outs[0])
+    assert O.rel_error(outs[0], O.cpu_solve(A, B, d)) <= TOL64
