@@ -26,7 +26,7 @@ from ._lib import BSSError, NotSPDError  # noqa: F401
 __all__ = [
     "BlockTriDiagData_batched", "BlockTriDiagData_seq", "initialize_batched", "initialize_seq",
     "factorize_", "solve_", "factorize", "solve", "synchronize", "get_info", "residual",
-    "plan_reference", "BSSError", "NotSPDError",
+    "plan_reference", "BSSError", "NotSPDError", "MultiSystemBatch", "initialize_multi",
 ]
 
 
@@ -227,6 +227,114 @@ def residual(A_tensor, B_tensor, x_tensor, d_tensor, stream=None) -> float:
                                         ctypes.c_void_p(x_tensor.data_ptr()), ctypes.c_void_p(d_tensor.data_ptr()),
                                         _stream_ptr(stream), ctypes.byref(out)))
     return out.value
+
+
+class _BatchHandle:
+    """Owns a bss_batch*; destroyed when the last tensor view is gone."""
+
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                _lib.load().bss_batch_destroy(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+
+class MultiSystemBatch:
+    """Many independent block-tridiagonal systems of their own N, n and k,
+    factorized and solved together (no counterpart in the reference).
+
+    ``systems[s]`` has ``A_tensor`` (n x n x N), ``B_tensor`` (n x n x (N-1))
+    and ``d_tensor`` (n x k x N): column-major views of library memory, laid
+    out like a single system's.  ``factorize()`` / ``solve()`` run every
+    system; ``d_tensor`` then holds each system's solution."""
+
+    class _System:
+        pass
+
+    def __init__(self, handle: _BatchHandle, nsys: int, torch_dtype):
+        torch = _torch()
+        L = _lib.load()
+        self._h = handle
+        self.dtype = torch_dtype
+        es = 8 if torch_dtype == torch.float64 else 4
+        ts = "<f8" if es == 8 else "<f4"
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self.systems = []
+        for s in range(nsys):
+            N = ctypes.c_int64()
+            n = ctypes.c_int64()
+            k = ctypes.c_int64()
+            _lib.check(L.bss_batch_get_dims(handle.ptr, s, ctypes.byref(N), ctypes.byref(n), ctypes.byref(k)))
+            A = ctypes.c_void_p()
+            B = ctypes.c_void_p()
+            d = ctypes.c_void_p()
+            _lib.check(L.bss_batch_get_tensors(handle.ptr, s, ctypes.byref(A), ctypes.byref(B), ctypes.byref(d)))
+            N, n, k = N.value, n.value, k.value
+            nn = n * n
+            sysv = MultiSystemBatch._System()
+            sysv.N, sysv.n, sysv.k, sysv.dtype = N, n, k, torch_dtype
+            sysv.A_tensor = torch.as_tensor(
+                _DevView(A.value, (n, n, N), (es, es * n, es * nn), ts, handle), device=dev)
+            sysv.B_tensor = torch.as_tensor(
+                _DevView(B.value, (n, n, max(N - 1, 0)), (es, es * n, es * nn), ts, handle), device=dev)
+            sysv.d_tensor = torch.as_tensor(
+                _DevView(d.value, (n, k, N), (es, es * n, es * n * k), ts, handle), device=dev)
+            self.systems.append(sysv)
+
+    @property
+    def handle(self):
+        return self._h.ptr
+
+    def __len__(self):
+        return len(self.systems)
+
+    def factorize(self, check: bool = False) -> None:
+        _lib.check(_lib.load().bss_batch_factorize(self.handle))
+        if check:
+            self.synchronize()
+
+    def solve(self, check: bool = False) -> None:
+        _lib.check(_lib.load().bss_batch_solve(self.handle))
+        if check:
+            self.synchronize()
+
+    def synchronize(self) -> None:
+        _lib.check(_lib.load().bss_batch_synchronize(self.handle))
+
+    def info(self, s: int) -> dict:
+        inf = _lib.Info()
+        _lib.check(_lib.load().bss_batch_get_info(self.handle, int(s), ctypes.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in _lib.Info._fields_}
+
+
+def initialize_multi(Ns, ns, ks=None, T=None, *, precision: str = "plain", max_refine: int = 10,
+                     tol: float = 1e-12, use_graphs: bool = True, stream=None) -> MultiSystemBatch:
+    """Create a batch of independent systems: system s has Ns[s] blocks of
+    size ns[s] (<= 64) and ks[s] right-hand sides (default 1)."""
+    torch = _torch()
+    code, tdt = _dtype_code(torch.float64 if T is None else T)
+    nsys = len(Ns)
+    if ks is None:
+        ks = [1] * nsys
+    if not (len(ns) == nsys and len(ks) == nsys) or nsys < 1:
+        raise ValueError("Ns, ns and ks must be non-empty and of equal length")
+    o = _lib.default_options()
+    o.precision = {"plain": _lib.BSS_PRECISION_PLAIN, "mixed": _lib.BSS_PRECISION_MIXED}[precision]
+    o.max_refine = int(max_refine)
+    o.tol = float(tol)
+    o.use_graphs = 1 if use_graphs else 0
+    arr = ctypes.c_int64 * nsys
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    torch.cuda.current_device()
+    _lib.check(L.bss_batch_create(nsys, arr(*map(int, Ns)), arr(*map(int, ns)), arr(*map(int, ks)), code,
+                                  _stream_ptr(stream), ctypes.byref(o), ctypes.byref(h)))
+    return MultiSystemBatch(_BatchHandle(h.value), nsys, tdt)
 
 
 def plan_reference(N: int):

@@ -36,7 +36,8 @@ EXPORTS = (
     "bss_get_tensors", "bss_get_dims", "bss_factorize", "bss_solve", "bss_synchronize",
     "bss_get_info", "bss_last_error_string", "bss_plan_reference", "bss_residual",
     "bss_factorize_levels", "bss_get_level", "bss_factor_solve_noalloc", "bss_kernel_launches",
-    "bss_version",
+    "bss_version", "bss_batch_create", "bss_batch_destroy", "bss_batch_get_tensors", "bss_batch_get_dims",
+    "bss_batch_factorize", "bss_batch_solve", "bss_batch_synchronize", "bss_batch_get_info",
 )
 
 
@@ -49,6 +50,7 @@ class Options(ctypes.Structure):
         ("seq_cutoff", ctypes.c_int32),
         ("use_graphs", ctypes.c_int32),
         ("tol", ctypes.c_double),
+        ("chain_blocks", ctypes.c_int32),
     ]
 
 
@@ -112,6 +114,15 @@ def load(path: str | None = None):
     L.bss_kernel_launches.restype = ctypes.c_int64
     L.bss_version.argtypes = []
     L.bss_version.restype = ctypes.c_char_p
+    pi64 = ctypes.POINTER(i64)
+    L.bss_batch_create.argtypes = [i32, pi64, pi64, pi64, i32, vp, ctypes.POINTER(Options), ctypes.POINTER(vp)]
+    L.bss_batch_destroy.argtypes = [vp]
+    L.bss_batch_get_tensors.argtypes = [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    L.bss_batch_get_dims.argtypes = [vp, i32, pi64, pi64, pi64]
+    L.bss_batch_factorize.argtypes = [vp]
+    L.bss_batch_solve.argtypes = [vp]
+    L.bss_batch_synchronize.argtypes = [vp]
+    L.bss_batch_get_info.argtypes = [vp, i32, ctypes.POINTER(Info)]
     for name in EXPORTS:
         if name not in ("bss_default_options", "bss_last_error_string", "bss_version", "bss_kernel_launches"):
             getattr(L, name).restype = ctypes.c_int

@@ -18,94 +18,29 @@
 #include <string>
 #include <vector>
 
-#include "../../include/bss.h"
-#include "bss_launch.h"
+#include "bss_internal.h"
 
 using namespace bss;
 
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
 
-int fail(int code, const std::string &msg)
+int bss::fail(int code, const std::string &msg)
 {
     g_last_error = msg;
     return code;
 }
 
-}  // namespace
-
 void bss::set_last_error(const std::string &msg) { g_last_error = msg; }
 
-namespace {
-
-int cuda_fail(cudaError_t e, const char *what)
+int bss::cuda_fail(cudaError_t e, const char *what)
 {
     return fail(e == cudaErrorMemoryAllocation ? BSS_ERR_OOM : BSS_ERR_CUDA,
                 std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define BSS_CUDA(call)                                       \
-    do {                                                     \
-        cudaError_t e__ = (call);                            \
-        if (e__ != cudaSuccess) return cuda_fail(e__, #call); \
-    } while (0)
 
-enum Ty { F32 = 0, F64 = 1 };
-
-inline size_t tsize(int t) { return t == F64 ? 8 : 4; }
-
-// one level of the recursion (finest = 0; the last one is the sequential
-// coarsest level)
-struct Level {
-    long long N = 0;
-    long long Q = 0;  // partitions (0 for the sequential level)
-    bool seq = false;
-    int tin = F64;    // dtype of A/B as read by the factor kernel
-    int t = F64;      // dtype of factors, workspace and RHS at this level
-    void *A = nullptr, *B = nullptr;    // level system (input)
-    void *Af = nullptr, *Bf = nullptr;  // factor storage (== A/B when in place)
-    void *d = nullptr;                  // level RHS (t), n x k per block
-    void *Y = nullptr, *C = nullptr, *bvec = nullptr;
-};
-
-}  // namespace
-
-struct bss_handle {
-    long long N_user = 0, N = 0, n = 0, k = 0;
-    int dtype = F64;
-    bss_options opt{};
-    bool seq_api = false;
-    cudaStream_t stream = nullptr;
-    int device = 0;
-    char *arena = nullptr;
-    size_t arena_bytes = 0;
-    void *A = nullptr, *B = nullptr, *d = nullptr;  // user-visible tensors
-    std::vector<Level> levels;
-    // mixed precision workspace
-    void *c0 = nullptr;     // level-0 correction RHS (levels[0].t)
-    double *x64 = nullptr;  // FP64 solution accumulator
-    DevStatus *st = nullptr;
-    DevStatus *h_st = nullptr;  // pinned mirror
-    bool factored = false;
-    bool need_anorm = false;  // the next residual also computes ||T||_inf
-    int kc_max = 1;
-    bss_info info{};
-    int sticky = BSS_OK;
-    // CUDA graphs: the first call of each kind runs eagerly on `stream`; later
-    // calls replay a graph captured on cap_stream and launched on `stream`
-    cudaStream_t ls = nullptr;          // stream the launch code enqueues on
-    cudaStream_t cap_stream = nullptr;  // private capture streams
-    cudaStream_t cap_stream2 = nullptr;
-    cudaGraphExec_t g_factor = nullptr, g_solve = nullptr;
-    int n_factor = 0, n_solve = 0;
-    // kernels per replay (captured launches); mixed solve: prologue, loop
-    // body (residual + decision) and correction, combined at synchronize
-    long long k_factor = 0, k_solve = 0, k_pro = 0, k_body = 0, k_corr = 0;
-    long long graph_solves_unsynced = 0;        // device-loop solves launched since the last sync
-    unsigned long long iters_total_seen = 0;    // st->iters_total at the last sync
-    bool graph_solve_pending = false;   // a graph solve ran: read its outcome at synchronize
-};
 
 extern "C" void bss_default_options(bss_options *o)
 {
@@ -118,6 +53,7 @@ extern "C" void bss_default_options(bss_options *o)
     o->seq_cutoff = 0;
     o->use_graphs = 1;
     o->tol = 1e-12;
+    o->chain_blocks = 0;
 }
 
 extern "C" const char *bss_last_error_string(void) { return g_last_error.c_str(); }
@@ -244,7 +180,9 @@ int chain_ctas_per_sm(int tin, int t, int n)
     return chain_factor_ctas_per_sm<double, double>(n);
 }
 
-int build_handle(bss_handle *h)
+}  // namespace
+
+int bss::plan_handle(bss_handle *h)
 {
     const long long n = h->n, k = h->k, nn = n * n;
     const bool mixed = h->opt.precision == BSS_PRECISION_MIXED;
@@ -274,7 +212,6 @@ int build_handle(bss_handle *h)
             plan_auto(h->N, target, cutoff, Ns, Qs, coarsest);
         }
     }
-    // level list
     h->levels.clear();
     for (size_t l = 0; l < Ns.size(); ++l) {
         Level L;
@@ -295,96 +232,118 @@ int build_handle(bss_handle *h)
         h->levels.push_back(L);
     }
     const int nlev = (int)h->levels.size();
-
-    // arena layout
+    Layout &o = h->layout;
     ArenaPlan ap;
-    const size_t offA = ap.take((size_t)h->N * nn * tsize(D));
-    const size_t offB = ap.take((size_t)std::max(h->N - 1, 1LL) * nn * tsize(D));
-    const size_t offd = ap.take((size_t)h->N * n * k * tsize(D));
-    std::vector<size_t> oA(nlev), oB(nlev), od(nlev), oAf(nlev), oBf(nlev), oY(nlev), oC(nlev), ob(nlev);
+    o.A = ap.take((size_t)h->N * nn * tsize(D));
+    o.B = ap.take((size_t)std::max(h->N - 1, 1LL) * nn * tsize(D));
+    o.d = ap.take((size_t)h->N * n * k * tsize(D));
+    o.lA.assign(nlev, 0);
+    o.lB.assign(nlev, 0);
+    o.ld.assign(nlev, 0);
+    o.lAf.assign(nlev, 0);
+    o.lBf.assign(nlev, 0);
+    o.lY.assign(nlev, 0);
+    o.lC.assign(nlev, 0);
+    o.lb.assign(nlev, 0);
     for (int l = 0; l < nlev; ++l) {
         Level &L = h->levels[l];
         const size_t ts = tsize(L.t);
         if (l > 0) {
-            oA[l] = ap.take((size_t)L.N * nn * ts);
-            oB[l] = ap.take((size_t)std::max(L.N - 1, 1LL) * nn * ts);
-            od[l] = ap.take((size_t)L.N * n * k * ts);
+            o.lA[l] = ap.take((size_t)L.N * nn * ts);
+            o.lB[l] = ap.take((size_t)std::max(L.N - 1, 1LL) * nn * ts);
+            o.ld[l] = ap.take((size_t)L.N * n * k * ts);
         }
-        const bool separate_factor = (l == 0) && (mixed);
-        if (separate_factor) {
-            oAf[l] = ap.take((size_t)L.N * nn * ts);
-            oBf[l] = ap.take((size_t)std::max(L.N - 1, 1LL) * nn * ts);
+        if (l == 0 && mixed) {
+            o.lAf[l] = ap.take((size_t)L.N * nn * ts);
+            o.lBf[l] = ap.take((size_t)std::max(L.N - 1, 1LL) * nn * ts);
         }
         if (!L.seq) {
-            oY[l] = ap.take((size_t)L.N * nn * ts);
-            oC[l] = ap.take((size_t)L.Q * 3 * nn * ts);
-            ob[l] = ap.take((size_t)L.Q * 2 * n * std::max(1LL, (long long)h->kc_max) * ts);
+            o.lY[l] = ap.take((size_t)L.N * nn * ts);
+            o.lC[l] = ap.take((size_t)L.Q * 3 * nn * ts);
+            o.lb[l] = ap.take((size_t)L.Q * 2 * n * std::max(1LL, (long long)h->kc_max) * ts);
         }
     }
-    size_t oc0 = 0, ox = 0;
     if (mixed) {
-        oc0 = ap.take((size_t)h->N * n * k * tsize(h->levels[0].t));
-        ox = ap.take((size_t)h->N * n * k * 8);
+        o.c0 = ap.take((size_t)h->N * n * k * tsize(h->levels[0].t));
+        o.x = ap.take((size_t)h->N * n * k * 8);
     }
-    const size_t ost = ap.take(sizeof(DevStatus));
+    o.st = ap.take(sizeof(DevStatus));
     h->arena_bytes = ap.bytes;
-    cudaError_t e = cudaMalloc((void **)&h->arena, h->arena_bytes);
-    if (e != cudaSuccess) {
-        h->arena = nullptr;
-        return cuda_fail(e, "cudaMalloc(arena)");
-    }
-    char *base = h->arena;
-    BSS_CUDA(cudaMemsetAsync(base, 0, h->arena_bytes, h->stream));
-    h->A = base + offA;
-    h->B = base + offB;
-    h->d = base + offd;
-    for (int l = 0; l < nlev; ++l) {
-        Level &L = h->levels[l];
-        if (l == 0) {
-            L.A = h->A;
-            L.B = h->B;
-        } else {
-            L.A = base + oA[l];
-            L.B = base + oB[l];
-            L.d = base + od[l];
-        }
-        if ((l == 0) && mixed) {
-            L.Af = base + oAf[l];
-            L.Bf = base + oBf[l];
-        } else {
-            L.Af = L.A;
-            L.Bf = L.B;
-        }
-        if (!L.seq) {
-            L.Y = base + oY[l];
-            L.C = base + oC[l];
-            L.bvec = base + ob[l];
-        }
-    }
-    if (mixed) {
-        h->c0 = base + oc0;
-        h->x64 = reinterpret_cast<double *>(base + ox);
-        h->levels[0].d = h->c0;
-    } else {
-        h->levels[0].d = h->d;
-    }
-    h->st = reinterpret_cast<DevStatus *>(base + ost);
-    BSS_CUDA(cudaMallocHost((void **)&h->h_st, sizeof(DevStatus)));
-    std::memset(h->h_st, 0, sizeof(DevStatus));
-    // identity padding of A (gpu_batched.jl:177-179: blocks N..N_use, 1-based)
-    if (!h->seq_api) {
-        const long long first = h->N_user - 1;
-        cudaError_t ie = (D == F64)
-                             ? launch_init_identity<double>((double *)h->A, first, h->N, (int)n, h->stream)
-                             : launch_init_identity<float>((float *)h->A, first, h->N, (int)n, h->stream);
-        if (ie != cudaSuccess) return cuda_fail(ie, "init_identity");
-    }
     h->info.failed_block = -1;
     h->info.failed_level = -1;
     h->info.rel_residual = -1.0;
     h->info.levels = nlev - 1;
     h->info.coarsest_blocks = coarsest;
     return BSS_OK;
+}
+
+int bss::bind_handle(bss_handle *h, char *base, bool alloc_host_status)
+{
+    const bool mixed = h->opt.precision == BSS_PRECISION_MIXED;
+    const Layout &o = h->layout;
+    const int nlev = (int)h->levels.size();
+    BSS_CUDA(cudaMemsetAsync(base, 0, h->arena_bytes, h->stream));
+    h->A = base + o.A;
+    h->B = base + o.B;
+    h->d = base + o.d;
+    for (int l = 0; l < nlev; ++l) {
+        Level &L = h->levels[l];
+        if (l == 0) {
+            L.A = h->A;
+            L.B = h->B;
+        } else {
+            L.A = base + o.lA[l];
+            L.B = base + o.lB[l];
+            L.d = base + o.ld[l];
+        }
+        if (l == 0 && mixed) {
+            L.Af = base + o.lAf[l];
+            L.Bf = base + o.lBf[l];
+        } else {
+            L.Af = L.A;
+            L.Bf = L.B;
+        }
+        if (!L.seq) {
+            L.Y = base + o.lY[l];
+            L.C = base + o.lC[l];
+            L.bvec = base + o.lb[l];
+        }
+    }
+    if (mixed) {
+        h->c0 = base + o.c0;
+        h->x64 = reinterpret_cast<double *>(base + o.x);
+        h->levels[0].d = h->c0;
+    } else {
+        h->levels[0].d = h->d;
+    }
+    h->st = reinterpret_cast<DevStatus *>(base + o.st);
+    if (alloc_host_status) {
+        BSS_CUDA(cudaMallocHost((void **)&h->h_st, sizeof(DevStatus)));
+        std::memset(h->h_st, 0, sizeof(DevStatus));
+    }
+    // identity padding of A (gpu_batched.jl:177-179: blocks N..N_use, 1-based)
+    if (!h->seq_api && h->N > h->N_user - 1) {
+        const long long first = h->N_user - 1;
+        cudaError_t ie = (h->dtype == F64)
+                             ? launch_init_identity<double>((double *)h->A, first, h->N, (int)h->n, h->stream)
+                             : launch_init_identity<float>((float *)h->A, first, h->N, (int)h->n, h->stream);
+        if (ie != cudaSuccess) return cuda_fail(ie, "init_identity");
+    }
+    return BSS_OK;
+}
+
+namespace {
+
+int build_handle(bss_handle *h)
+{
+    int rc = plan_handle(h);
+    if (rc) return rc;
+    cudaError_t e = cudaMalloc((void **)&h->arena, h->arena_bytes);
+    if (e != cudaSuccess) {
+        h->arena = nullptr;
+        return cuda_fail(e, "cudaMalloc(arena)");
+    }
+    return bind_handle(h, h->arena, true);
 }
 
 int check_dims(int64_t N, int64_t n, int64_t k, int32_t dtype)
@@ -470,7 +429,7 @@ extern "C" int bss_destroy(bss_handle *h)
     if (h->g_solve) cudaGraphExecDestroy(h->g_solve);
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     if (h->cap_stream2) cudaStreamDestroy(h->cap_stream2);
-    if (h->arena) cudaFree(h->arena);
+    if (h->arena && !h->external_arena) cudaFree(h->arena);
     if (h->h_st) cudaFreeHost(h->h_st);
     delete h;
     return BSS_OK;
@@ -503,6 +462,14 @@ namespace {
 template <class Tin, class T>
 cudaError_t factor_level(bss_handle *h, int l)
 {
+    return launch_chain_factor<Tin, T>(make_factor_args<Tin, T>(h, l), h->ls);
+}
+
+}  // namespace
+
+template <class Tin, class T>
+ChainFactorArgs<Tin, T> bss::make_factor_args(bss_handle *h, int l)
+{
     Level &L = h->levels[l];
     ChainFactorArgs<Tin, T> a;
     a.A_in = (const Tin *)L.A;
@@ -517,8 +484,13 @@ cudaError_t factor_level(bss_handle *h, int l)
     a.seq = L.seq ? 1 : 0;
     a.level = l;
     a.st = h->st;
-    return launch_chain_factor<Tin, T>(a, h->ls);
+    return a;
 }
+template ChainFactorArgs<double, double> bss::make_factor_args<double, double>(bss_handle *, int);
+template ChainFactorArgs<double, float> bss::make_factor_args<double, float>(bss_handle *, int);
+template ChainFactorArgs<float, float> bss::make_factor_args<float, float>(bss_handle *, int);
+
+namespace {
 
 cudaError_t assemble_level(bss_handle *h, int l)
 {
@@ -652,8 +624,10 @@ extern "C" int bss_get_level(bss_handle *h, int32_t level, int64_t *N, int64_t *
 // ---------------------------------------------------------------------------
 namespace {
 
+}  // namespace
+
 template <class T>
-SolveArgs<T> solve_args(bss_handle *h, int l, int j0, int kc)
+SolveArgs<T> bss::make_solve_args(bss_handle *h, int l, int j0, int kc)
 {
     Level &L = h->levels[l];
     SolveArgs<T> a;
@@ -671,6 +645,16 @@ SolveArgs<T> solve_args(bss_handle *h, int l, int j0, int kc)
     a.kc = kc;
     a.seq = L.seq ? 1 : 0;
     return a;
+}
+template SolveArgs<double> bss::make_solve_args<double>(bss_handle *, int, int, int);
+template SolveArgs<float> bss::make_solve_args<float>(bss_handle *, int, int, int);
+
+namespace {
+
+template <class T>
+SolveArgs<T> solve_args(bss_handle *h, int l, int j0, int kc)
+{
+    return make_solve_args<T>(h, l, j0, kc);
 }
 
 cudaError_t fwd_level(bss_handle *h, int l, int j0, int kc)

@@ -517,8 +517,9 @@ constexpr size_t chain_factor_smem()
     return (size_t)(6 * Geo<T, NB>::SLOT + NB) * sizeof(T) + 16;
 }
 
+// one partition's chain (or the whole sequential chain when g.seq)
 template <class Tin, class T, int NB>
-__global__ void __launch_bounds__(Tile<NB>::THREADS, sizeof(T) == 4 ? 2 : 1) chain_factor_kernel(ChainFactorArgs<Tin, T> g)
+__device__ __forceinline__ void chain_factor_body(const ChainFactorArgs<Tin, T> &g, const long long p)
 {
     using TL = Tile<NB>;
     constexpr int LD = Geo<T, NB>::LD;
@@ -538,7 +539,6 @@ __global__ void __launch_bounds__(Tile<NB>::THREADS, sizeof(T) == 4 ? 2 : 1) cha
     const int n = g.n;
     const long long nn = (long long)n * n;
     const bool seq = g.seq != 0;
-    const long long p = blockIdx.x;
 
     long long first, last, sL = 0;
     if (seq) {
@@ -629,6 +629,40 @@ __global__ void __launch_bounds__(Tile<NB>::THREADS, sizeof(T) == 4 ? 2 : 1) cha
         store_sym_global<T, NB>(Cp, accLL, n, ti, tj);
         store_sym_global<T, NB>(Cp + nn, accRR, n, ti, tj);
         store_tile_global<T, NB>(Cp + 2 * nn, accLR, n, ti, tj, T(1));
+    }
+}
+
+// work item of the batched (queue) kernels: descriptor index, partition
+struct WorkItem {
+    int desc;
+    int p;
+};
+
+template <class Tin, class T, int NB>
+__global__ void __launch_bounds__(Tile<NB>::THREADS, sizeof(T) == 4 ? 2 : 1) chain_factor_kernel(ChainFactorArgs<Tin, T> g)
+{
+    chain_factor_body<Tin, T, NB>(g, blockIdx.x);
+}
+
+// Persistent form for many systems: each CTA pulls (system, partition)
+// items from a device queue (longest chains first, placed so by the host)
+// until it is empty.  *head must be zero at launch.
+template <class Tin, class T, int NB>
+__global__ void __launch_bounds__(Tile<NB>::THREADS, sizeof(T) == 4 ? 2 : 1)
+    chain_factor_queue_kernel(const ChainFactorArgs<Tin, T> *__restrict__ descs, const WorkItem *__restrict__ items,
+                              int nitems, int *head)
+{
+    __shared__ int cur;
+    for (;;) {
+        if (threadIdx.x == 0) cur = atomicAdd(head, 1);
+        __syncthreads();
+        const int it = cur;
+        __syncthreads();
+        if (it >= nitems) break;
+        const WorkItem w = items[it];
+        const ChainFactorArgs<Tin, T> g = descs[w.desc];
+        chain_factor_body<Tin, T, NB>(g, w.p);
+        __syncthreads();
     }
 }
 
@@ -817,7 +851,7 @@ __device__ __forceinline__ void store_rhs(Tg *__restrict__ g, const T *s, long l
 // forward sweep of one partition; for the sequential (coarsest) level the
 // whole chain followed by its backward sweep.
 template <class T>
-__global__ void __launch_bounds__(SOLVE_THREADS) chain_fwd_kernel(SolveArgs<T> g)
+__device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long long p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = g.n, kc = g.kc;
@@ -830,7 +864,6 @@ __global__ void __launch_bounds__(SOLVE_THREADS) chain_fwd_kernel(SolveArgs<T> g
     T *sx = sbR + nkc;
     T *red = sx + nkc;
     const bool seq = g.seq != 0;
-    const long long p = blockIdx.x;
     long long first, last;
     if (seq) {
         first = 0;
@@ -913,6 +946,31 @@ __global__ void __launch_bounds__(SOLVE_THREADS) chain_fwd_kernel(SolveArgs<T> g
     cp_async_wait_all();
 }
 
+template <class T>
+__global__ void __launch_bounds__(SOLVE_THREADS) chain_fwd_kernel(SolveArgs<T> g)
+{
+    chain_fwd_body<T>(g, blockIdx.x);
+}
+
+template <class T>
+__global__ void __launch_bounds__(SOLVE_THREADS)
+    chain_fwd_queue_kernel(const SolveArgs<T> *__restrict__ descs, const WorkItem *__restrict__ items, int nitems,
+                           int *head)
+{
+    __shared__ int cur;
+    for (;;) {
+        if (threadIdx.x == 0) cur = atomicAdd(head, 1);
+        __syncthreads();
+        const int it = cur;
+        __syncthreads();
+        if (it >= nitems) break;
+        const WorkItem w = items[it];
+        const SolveArgs<T> g = descs[w.desc];
+        chain_fwd_body<T>(g, w.p);
+        __syncthreads();
+    }
+}
+
 // separator RHS: d'_s = d_{sep s} - bL(s) - bR(s-1)   (reference compute_schur_RHS!,
 // backbone_cuda.jl:159-171, and the gather gpu_batched.jl:251)
 template <class T, class Tn>
@@ -938,7 +996,7 @@ __global__ void assemble_rhs_kernel(const T *__restrict__ d, const T *__restrict
 // the level's separator slots (reference update_boundary! + the scatter
 // gpu_batched.jl:253, and cholesky_solve_batched! :257).
 template <class T, class Tsep>
-__global__ void __launch_bounds__(SOLVE_THREADS) chain_bwd_kernel(SolveArgs<T> g)
+__device__ __forceinline__ void chain_bwd_body(const SolveArgs<T> &g, const long long p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = g.n, kc = g.kc;
@@ -950,7 +1008,6 @@ __global__ void __launch_bounds__(SOLVE_THREADS) chain_bwd_kernel(SolveArgs<T> g
     T *sxn = sxL + nkc;
     T *sxt = sxn + nkc;
     T *red = sxt + nkc;
-    const long long p = blockIdx.x;
     const long long sL = (p * (g.N - 1)) / g.Q;
     const long long sR = ((p + 1) * (g.N - 1)) / g.Q;
     const long long first = sL + 1, last = sR - 1;
@@ -988,6 +1045,31 @@ __global__ void __launch_bounds__(SOLVE_THREADS) chain_bwd_kernel(SolveArgs<T> g
         __syncthreads();
     }
     cp_async_wait_all();
+}
+
+template <class T, class Tsep>
+__global__ void __launch_bounds__(SOLVE_THREADS) chain_bwd_kernel(SolveArgs<T> g)
+{
+    chain_bwd_body<T, Tsep>(g, blockIdx.x);
+}
+
+template <class T, class Tsep>
+__global__ void __launch_bounds__(SOLVE_THREADS)
+    chain_bwd_queue_kernel(const SolveArgs<T> *__restrict__ descs, const WorkItem *__restrict__ items, int nitems,
+                           int *head)
+{
+    __shared__ int cur;
+    for (;;) {
+        if (threadIdx.x == 0) cur = atomicAdd(head, 1);
+        __syncthreads();
+        const int it = cur;
+        __syncthreads();
+        if (it >= nitems) break;
+        const WorkItem w = items[it];
+        const SolveArgs<T> g = descs[w.desc];
+        chain_bwd_body<T, Tsep>(g, w.p);
+        __syncthreads();
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1091,11 +1173,10 @@ __device__ __forceinline__ void residual_rows(const T *__restrict__ Ag, const T 
 }
 
 template <class T, class Tr>
-__global__ void __launch_bounds__(RES_THREADS, 3) residual_kernel(const T *__restrict__ A, const T *__restrict__ B,
-                                                               const T *__restrict__ x, const T *__restrict__ d,
-                                                               Tr *__restrict__ r, long long N, int n, int ktot,
-                                                               int j0, int k, long long per_cta, int with_norm,
-                                                               DevStatus *st)
+__device__ __forceinline__ void residual_body(const T *__restrict__ A, const T *__restrict__ B,
+                                              const T *__restrict__ x, const T *__restrict__ d, Tr *__restrict__ r,
+                                              long long N, int n, int ktot, int j0, int k, long long b0_, long long b1_,
+                                              int with_norm, DevStatus *st)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int LDp = n + 1;
@@ -1114,8 +1195,8 @@ __global__ void __launch_bounds__(RES_THREADS, 3) residual_kernel(const T *__res
     const bool active = part < parts;
     const int c0 = active ? (part * n) / parts : 0, c1 = active ? ((part + 1) * n) / parts : 0;
     const long long nn = (long long)n * n;
-    const long long b0 = (long long)blockIdx.x * per_cta;
-    const long long b1 = (b0 + per_cta < N) ? b0 + per_cta : N;
+    const long long b0 = b0_;
+    const long long b1 = b1_ < N ? b1_ : N;
     if (b0 >= N) return;
     if (with_norm < 0) with_norm = st->need_anorm;  // graph mode: decided on the device
     double rmax = 0.0, xmax = 0.0, amax = 0.0;
@@ -1236,6 +1317,38 @@ __global__ void __launch_bounds__(RES_THREADS, 3) residual_kernel(const T *__res
     }
 }
 
+template <class T, class Tr>
+__global__ void __launch_bounds__(RES_THREADS, 3) residual_kernel(const T *__restrict__ A, const T *__restrict__ B,
+                                                               const T *__restrict__ x, const T *__restrict__ d,
+                                                               Tr *__restrict__ r, long long N, int n, int ktot,
+                                                               int j0, int k, long long per_cta, int with_norm,
+                                                               DevStatus *st)
+{
+    const long long b0 = (long long)blockIdx.x * per_cta;
+    residual_body<T, Tr>(A, B, x, d, r, N, n, ktot, j0, k, b0, b0 + per_cta, with_norm, st);
+}
+
+// many systems: one CTA per (system, block range) item
+template <class Tr>
+struct ResidualDesc {
+    const double *A, *B, *x, *d;
+    Tr *r;
+    long long N;
+    int n, k;
+    long long per_cta;
+    DevStatus *st;
+};
+
+template <class Tr>
+__global__ void __launch_bounds__(RES_THREADS, 3) residual_batch_kernel(const ResidualDesc<Tr> *__restrict__ descs,
+                                                                       const WorkItem *__restrict__ items)
+{
+    const WorkItem w = items[blockIdx.x];
+    const ResidualDesc<Tr> g = descs[w.desc];
+    const long long b0 = (long long)w.p * g.per_cta;
+    residual_body<double, Tr>(g.A, g.B, g.x, g.d, g.r, g.N, g.n, g.k, 0, g.k, b0, b0 + g.per_cta, -1, g.st);
+}
+
 // one refinement decision on the device (graph mode): relative residual,
 // convergence, and the two conditional-node values (loop again / apply a
 // correction) -- no host round trip per refinement step
@@ -1274,6 +1387,148 @@ static __global__ void relres_kernel(DevStatus *st, double tol)
         const double rel = den > 0.0 ? rn / den : 0.0;
         st->relres = rel;
         st->done = (rel <= tol) ? 1 : 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// many-system (batch) helpers: descriptor arrays + work items
+// ---------------------------------------------------------------------------
+constexpr int BATCH_CHUNK = 4096;  // elements per work item of the elementwise batch kernels
+
+template <class Tsrc, class T, class Tdst>
+struct AsmSchurDesc {
+    const Tsrc *A_src;
+    const T *C;
+    Tdst *A_next;
+    Tdst *B_next;
+    long long N, Q;
+    int n;
+};
+
+template <class Tsrc, class T, class Tdst>
+__global__ void assemble_schur_batch_kernel(const AsmSchurDesc<Tsrc, T, Tdst> *__restrict__ descs,
+                                            const WorkItem *__restrict__ items)
+{
+    const WorkItem w = items[blockIdx.x];
+    const AsmSchurDesc<Tsrc, T, Tdst> g = descs[w.desc];
+    const long long nn = (long long)g.n * g.n;
+    const long long totalA = (g.Q + 1) * nn, total = totalA + g.Q * nn;
+    const long long e0 = (long long)w.p * BATCH_CHUNK;
+    for (long long e = e0 + threadIdx.x; e < total && e < e0 + BATCH_CHUNK; e += blockDim.x) {
+        if (e < totalA) {
+            const long long s = e / nn, q = e % nn;
+            const long long blk = (s * (g.N - 1)) / g.Q;
+            double v = (double)g.A_src[blk * nn + q];
+            if (s < g.Q) v -= (double)g.C[s * 3 * nn + q];
+            if (s > 0) v -= (double)g.C[(s - 1) * 3 * nn + nn + q];
+            g.A_next[e] = (Tdst)v;
+        } else {
+            const long long f = e - totalA;
+            const long long s = f / nn, q = f % nn;
+            g.B_next[f] = (Tdst)(-g.C[s * 3 * nn + 2 * nn + q]);
+        }
+    }
+}
+
+template <class T, class Tn>
+struct AsmRhsDesc {
+    const T *d;
+    const T *bvec;
+    Tn *dn;
+    long long N, Q;
+    int n, k, j0, kc;
+};
+
+template <class T, class Tn>
+__global__ void assemble_rhs_batch_kernel(const AsmRhsDesc<T, Tn> *__restrict__ descs,
+                                          const WorkItem *__restrict__ items)
+{
+    const WorkItem w = items[blockIdx.x];
+    const AsmRhsDesc<T, Tn> g = descs[w.desc];
+    const long long per = (long long)g.n * g.kc;
+    const long long total = (g.Q + 1) * per;
+    const long long e0 = (long long)w.p * BATCH_CHUNK;
+    for (long long e = e0 + threadIdx.x; e < total && e < e0 + BATCH_CHUNK; e += blockDim.x) {
+        const long long s = e / per, q = e % per;
+        const long long blk = (s * (g.N - 1)) / g.Q;
+        const long long off = (long long)g.j0 * g.n + q;
+        double v = (double)g.d[blk * (long long)g.n * g.k + off];
+        if (s < g.Q) v -= (double)g.bvec[s * 2 * per + q];
+        if (s > 0) v -= (double)g.bvec[(s - 1) * 2 * per + per + q];
+        g.dn[s * (long long)g.n * g.k + off] = (Tn)v;
+    }
+}
+
+// per-system vector operations of the batched refinement loop
+enum { VEC_ABSMAX = 0, VEC_TO_CORR = 1, VEC_SET = 2, VEC_ADD = 3, VEC_COPY_OUT = 4 };
+
+template <class Tc>
+struct VecDesc {
+    double *x;           // FP64 solution accumulator
+    Tc *c;               // correction / RHS in the factor precision
+    double *d;           // the user's FP64 right-hand side (solution on exit)
+    long long count;
+    DevStatus *st;
+};
+
+template <class Tc>
+__global__ void vec_batch_kernel(const VecDesc<Tc> *__restrict__ descs, const WorkItem *__restrict__ items, int op)
+{
+    const WorkItem w = items[blockIdx.x];
+    const VecDesc<Tc> g = descs[w.desc];
+    const long long e0 = (long long)w.p * BATCH_CHUNK;
+    double m = 0.0;
+    for (long long e = e0 + threadIdx.x; e < g.count && e < e0 + BATCH_CHUNK; e += blockDim.x) {
+        switch (op) {
+        case VEC_ABSMAX: m = fmax(m, fabs(g.d[e])); break;
+        case VEC_TO_CORR: g.c[e] = (Tc)g.d[e]; break;
+        case VEC_SET: g.x[e] = (double)g.c[e]; break;
+        case VEC_ADD: g.x[e] += (double)g.c[e]; break;
+        default: g.d[e] = g.x[e]; break;
+        }
+    }
+    if (op == VEC_ABSMAX) {
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&g.st->dnorm, m);
+    }
+}
+
+// per-system decision of the batched refinement loop; *any_cont collects
+// "some system still needs a correction"
+static __global__ void batch_decide_kernel(DevStatus *const *__restrict__ sts, int nsys, double tol, int max_refine,
+                                    int *any_cont)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys) return;
+    DevStatus *st = sts[s];
+    const double rn = __longlong_as_double((long long)st->rnorm);
+    const double xn = __longlong_as_double((long long)st->xnorm);
+    const double dn = __longlong_as_double((long long)st->dnorm);
+    const double an = __longlong_as_double((long long)st->anorm);
+    const double den = an * xn + dn;
+    const double rel = den > 0.0 ? rn / den : 0.0;
+    const int done = (rel <= tol) ? 1 : 0;
+    st->relres = rel;
+    st->done = done;
+    st->need_anorm = 0;
+    st->rnorm = 0ULL;
+    st->xnorm = 0ULL;
+    if (!done && st->iters < max_refine) {
+        st->iters += 1;
+        st->iters_total += 1;
+        atomicOr(any_cont, 1);
+    }
+}
+
+static __global__ void batch_set_conditional_kernel(int *any_cont, int *round, int max_refine,
+                                                    cudaGraphConditionalHandle hloop, cudaGraphConditionalHandle hcorr)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const int cont = (*any_cont != 0 && *round < max_refine) ? 1 : 0;
+        *any_cont = 0;
+        *round += 1;
+        cudaGraphSetConditional(hloop, (unsigned)cont);
+        cudaGraphSetConditional(hcorr, (unsigned)cont);
     }
 }
 

@@ -58,6 +58,10 @@ typedef struct {
     int32_t seq_cutoff;        /* auto plan: coarsest level size (0 = auto)        */
     int32_t use_graphs;        /* capture factorize/solve into CUDA graphs (1)     */
     double tol;                /* mixed: target relative residual (default 1e-12)  */
+    int32_t chain_blocks;      /* batch: blocks per partition at the finest level of
+                                  every system (0 = auto per n and precision); a
+                                  system's plan depends only on its own N, n and
+                                  this value, never on the other systems        */
 } bss_options;
 
 typedef struct {
@@ -174,6 +178,32 @@ int bss_get_level(bss_handle *h, int32_t level, int64_t *N, int64_t *Q, void **A
 #define BSS_NOALLOC_SCRATCH_BYTES (8u << 20)
 int bss_factor_solve_noalloc(int64_t N, int64_t n, int64_t k, int32_t dtype, void *A, void *B, void *d,
                              void *stream);
+
+/* ---- many independent systems in one batch --------------------------------
+ * No counterpart in the reference (its batching is over the partitions of
+ * ONE system, src/gpu_batched.jl:184-258).  nsys systems of their own N[s],
+ * n[s] (<= 64) and k[s] share one device arena; each recursion level of all
+ * systems runs as one persistent launch per block-size class whose CTAs pull
+ * (system, partition) items from a device work queue, longest chains first.
+ * Systems are not padded (tensors hold exactly N[s] blocks).  Tensors per
+ * system come from bss_batch_get_tensors (same layout as a handle's).  With
+ * opt->precision = BSS_PRECISION_MIXED (FP64 tensors) every system is
+ * refined to opt->tol; the refinement loop runs until all systems converge
+ * or max_refine.  factorize/solve are asynchronous on `stream` and replay
+ * CUDA graphs after their first call when opt->use_graphs.
+ * bss_batch_synchronize waits and returns BSS_ERR_NOT_SPD (first failing
+ * system) or BSS_ERR_NOT_CONVERGED; bss_batch_get_info gives each system's
+ * outcome. */
+typedef struct bss_batch bss_batch;
+int bss_batch_create(int32_t nsys, const int64_t *N, const int64_t *n, const int64_t *k, int32_t dtype,
+                     void *stream, const bss_options *opt, bss_batch **out);
+int bss_batch_destroy(bss_batch *b);
+int bss_batch_get_tensors(bss_batch *b, int32_t sys, void **A, void **B, void **d);
+int bss_batch_get_dims(bss_batch *b, int32_t sys, int64_t *N, int64_t *n, int64_t *k);
+int bss_batch_factorize(bss_batch *b);
+int bss_batch_solve(bss_batch *b);
+int bss_batch_synchronize(bss_batch *b);
+int bss_batch_get_info(bss_batch *b, int32_t sys, bss_info *info);
 
 /* Number of CUDA kernels this library has launched in this process, over
  * all handles (no counterpart in the reference; benchmarks report it). */
