@@ -351,8 +351,8 @@ int check_dims(int64_t N, int64_t n, int64_t k, int32_t dtype)
     if (N < 1 || n < 1 || k < 1) return fail(BSS_ERR_ARG, "N, n and k must be >= 1");
     if (dtype != BSS_F32 && dtype != BSS_F64) return fail(BSS_ERR_ARG, "dtype must be BSS_F32 or BSS_F64");
     if (tile_for((int)n) == 0)
-        return fail(BSS_ERR_UNSUPPORTED, "block size n=" + std::to_string(n) + " exceeds the fused-kernel limit " +
-                                             std::to_string(MAX_FUSED_N));
+        return fail(BSS_ERR_UNSUPPORTED, "block size n=" + std::to_string(n) + " exceeds the limit " +
+                                             std::to_string(MAX_WIDE_N));
     return BSS_OK;
 }
 
@@ -397,6 +397,10 @@ extern "C" int bss_create_batched(int64_t N, int64_t n, int64_t k, int32_t dtype
     if (h->opt.precision == BSS_PRECISION_MIXED && dtype != BSS_F64) {
         delete h;
         return fail(BSS_ERR_ARG, "mixed precision needs FP64 tensors");
+    }
+    if (h->opt.precision == BSS_PRECISION_MIXED && residual_smem_bytes<double>((int)n, 1) > (size_t)200 * 1024) {
+        delete h;
+        return fail(BSS_ERR_UNSUPPORTED, "mixed precision supports n <= 128 (FP64 residual kernel)");
     }
     if (h->opt.max_refine < 0) h->opt.max_refine = 0;
     h->N_user = N;

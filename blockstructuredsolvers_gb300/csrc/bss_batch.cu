@@ -17,6 +17,7 @@
 #include <cstring>
 #include <functional>
 #include <numeric>
+#include <string>
 #include <vector>
 
 #include "bss_internal.h"
@@ -56,7 +57,7 @@ inline int grid1d(int n) { return (n + 127) / 128; }
 
 struct Step {
     std::function<cudaError_t(cudaStream_t)> run;
-    int kernels = 1;  // kernels this step launches
+    std::string what;  // kernel and launch shape, for error messages
 };
 
 }  // namespace
@@ -137,10 +138,29 @@ cudaError_t queue_factor_nb(const ChainFactorArgs<Tin, T> *descs, const WorkItem
 }
 
 template <class Tin, class T>
+cudaError_t queue_factor_wide(const ChainFactorArgs<Tin, T> *descs, const WorkItem *items, int nitems, int *head,
+                              int sms, cudaStream_t s)
+{
+    const size_t smem = wide_factor_smem<T>();
+    auto kern = wide_chain_factor_queue_kernel<Tin, T>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, WIDE_THREADS, smem);
+    int grid = std::max(1, std::min(nitems, sms * std::max(per, 1)));
+    e = cudaMemsetAsync(head, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, WIDE_THREADS, smem, s>>>(descs, items, nitems, head);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class Tin, class T>
 cudaError_t queue_factor(int nb, const ChainFactorArgs<Tin, T> *descs, const WorkItem *items, int nitems, int *head,
                          int sms, cudaStream_t s)
 {
     switch (nb) {
+    case WIDE_CLASS: return queue_factor_wide<Tin, T>(descs, items, nitems, head, sms, s);
     case 16: return queue_factor_nb<Tin, T, 16>(descs, items, nitems, head, sms, s);
     case 32: return queue_factor_nb<Tin, T, 32>(descs, items, nitems, head, sms, s);
     default: return queue_factor_nb<Tin, T, 64>(descs, items, nitems, head, sms, s);
@@ -149,9 +169,9 @@ cudaError_t queue_factor(int nb, const ChainFactorArgs<Tin, T> *descs, const Wor
 
 template <class T>
 cudaError_t queue_fwd(const SolveArgs<T> *descs, const WorkItem *items, int nitems, int *head, size_t smem, int sms,
-                      cudaStream_t s)
+                      bool staged, cudaStream_t s)
 {
-    auto kern = chain_fwd_queue_kernel<T>;
+    auto kern = staged ? chain_fwd_queue_kernel<T, true> : chain_fwd_queue_kernel<T, false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per = 1;
@@ -166,9 +186,9 @@ cudaError_t queue_fwd(const SolveArgs<T> *descs, const WorkItem *items, int nite
 
 template <class T, class Tsep>
 cudaError_t queue_bwd(const SolveArgs<T> *descs, const WorkItem *items, int nitems, int *head, size_t smem, int sms,
-                      cudaStream_t s)
+                      bool staged, cudaStream_t s)
 {
-    auto kern = chain_bwd_queue_kernel<T, Tsep>;
+    auto kern = staged ? chain_bwd_queue_kernel<T, Tsep, true> : chain_bwd_queue_kernel<T, Tsep, false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per = 1;
@@ -193,7 +213,7 @@ template <class Tin, class T>
 void plan_factor_level(Builder &B, int level, bool coarsest)
 {
     bss_batch *b = B.b;
-    for (int nb : {16, 32, 64}) {
+    for (int nb : {16, 32, 64, (int)WIDE_CLASS}) {
         std::vector<ChainFactorArgs<Tin, T>> descs;
         std::vector<WorkItem> items;
         std::vector<long long> len;
@@ -225,6 +245,7 @@ void plan_factor_level(Builder &B, int level, bool coarsest)
         const int sms = b->sms;
         B.factor.push_back([=](char *base) {
             Step st;
+            st.what = std::string("plan_factor_level") + " items=" + std::to_string(ni);
             st.run = [=](cudaStream_t s) {
                 return queue_factor<Tin, T>(nb, (const ChainFactorArgs<Tin, T> *)(base + od),
                                             (const WorkItem *)(base + oi), ni, (int *)(base + oh), sms, s);
@@ -259,6 +280,7 @@ void plan_asm_schur(Builder &B, int level)
     const int ni = (int)items.size();
     B.factor.push_back([=](char *base) {
         Step st;
+        st.what = std::string("plan_asm_schur") + " items=" + std::to_string(ni);
         st.run = [=](cudaStream_t s) {
             assemble_schur_batch_kernel<Tsrc, T, Tdst><<<ni, 256, 0, s>>>(
                 (const AsmSchurDesc<Tsrc, T, Tdst> *)(base + od), (const WorkItem *)(base + oi));
@@ -271,7 +293,7 @@ void plan_asm_schur(Builder &B, int level)
 
 // forward sweeps (and the coarsest level's full solve) of one level
 template <class T>
-void plan_fwd(Builder &B, int level, bool coarsest, std::vector<std::function<Step(char *)>> &dst)
+void plan_fwd(Builder &B, int level, bool coarsest, bool staged, std::vector<std::function<Step(char *)>> &dst)
 {
     bss_batch *b = B.b;
     std::vector<SolveArgs<T>> descs;
@@ -285,9 +307,10 @@ void plan_fwd(Builder &B, int level, bool coarsest, std::vector<std::function<St
         if (l >= L) continue;
         const Level &lv = h->levels[l];
         if (lv.seq != coarsest || (lv.t == F64) != std::is_same<T, double>::value) continue;
+        if (solve_staged<T>((int)h->n, (int)h->k) != staged) continue;
         const int di = (int)descs.size();
         descs.push_back(make_solve_args<T>(h, l, 0, (int)h->k));
-        smem = std::max(smem, solve_smem_bytes<T>((int)h->n, (int)h->k));
+        smem = std::max(smem, solve_smem_bytes<T>((int)h->n, (int)h->k, staged));
         const long long q = lv.seq ? 1 : lv.Q;
         for (long long p = 0; p < q; ++p) {
             items.push_back(WorkItem{di, (int)p});
@@ -305,9 +328,10 @@ void plan_fwd(Builder &B, int level, bool coarsest, std::vector<std::function<St
     const int sms = b->sms;
     dst.push_back([=](char *base) {
         Step st;
+        st.what = std::string("plan_fwd") + " items=" + std::to_string(ni) + " smem=" + std::to_string(smem) + (staged ? " staged" : " direct");
         st.run = [=](cudaStream_t s) {
             return queue_fwd<T>((const SolveArgs<T> *)(base + od), (const WorkItem *)(base + oi), ni,
-                                (int *)(base + oh), smem, sms, s);
+                                (int *)(base + oh), smem, sms, staged, s);
         };
         return st;
     });
@@ -337,6 +361,7 @@ void plan_asm_rhs(Builder &B, int level, std::vector<std::function<Step(char *)>
     const int ni = (int)items.size();
     dst.push_back([=](char *base) {
         Step st;
+        st.what = std::string("plan_asm_rhs") + " items=" + std::to_string(ni);
         st.run = [=](cudaStream_t s) {
             assemble_rhs_batch_kernel<T, Tn><<<ni, 256, 0, s>>>((const AsmRhsDesc<T, Tn> *)(base + od),
                                                                (const WorkItem *)(base + oi));
@@ -348,7 +373,7 @@ void plan_asm_rhs(Builder &B, int level, std::vector<std::function<Step(char *)>
 }
 
 template <class T, class Tsep>
-void plan_bwd(Builder &B, int level, std::vector<std::function<Step(char *)>> &dst)
+void plan_bwd(Builder &B, int level, bool staged, std::vector<std::function<Step(char *)>> &dst)
 {
     bss_batch *b = B.b;
     std::vector<SolveArgs<T>> descs;
@@ -361,9 +386,10 @@ void plan_bwd(Builder &B, int level, std::vector<std::function<Step(char *)>> &d
         const Level &L = h->levels[level], &X = h->levels[level + 1];
         if ((L.t == F64) != std::is_same<T, double>::value || (X.t == F64) != std::is_same<Tsep, double>::value)
             continue;
+        if (solve_staged<T>((int)h->n, (int)h->k) != staged) continue;
         const int di = (int)descs.size();
         descs.push_back(make_solve_args<T>(h, level, 0, (int)h->k));
-        smem = std::max(smem, solve_smem_bytes<T>((int)h->n, (int)h->k));
+        smem = std::max(smem, solve_smem_bytes<T>((int)h->n, (int)h->k, staged));
         for (long long p = 0; p < L.Q; ++p) {
             items.push_back(WorkItem{di, (int)p});
             len.push_back((L.N - 1) / L.Q);
@@ -380,9 +406,10 @@ void plan_bwd(Builder &B, int level, std::vector<std::function<Step(char *)>> &d
     const int sms = b->sms;
     dst.push_back([=](char *base) {
         Step st;
+        st.what = std::string("plan_bwd") + " items=" + std::to_string(ni) + " smem=" + std::to_string(smem) + (staged ? " staged" : " direct");
         st.run = [=](cudaStream_t s) {
             return queue_bwd<T, Tsep>((const SolveArgs<T> *)(base + od), (const WorkItem *)(base + oi), ni,
-                                      (int *)(base + oh), smem, sms, s);
+                                      (int *)(base + oh), smem, sms, staged, s);
         };
         return st;
     });
@@ -392,19 +419,24 @@ void plan_bwd(Builder &B, int level, std::vector<std::function<Step(char *)>> &d
 void plan_chain_solve(Builder &B, int maxpart, std::vector<std::function<Step(char *)>> &dst)
 {
     for (int l = 0; l < maxpart; ++l) {
-        plan_fwd<float>(B, l, false, dst);
-        plan_fwd<double>(B, l, false, dst);
+        for (bool st : {true, false}) {
+            plan_fwd<float>(B, l, false, st, dst);
+            plan_fwd<double>(B, l, false, st, dst);
+        }
         plan_asm_rhs<float, float>(B, l, dst);
         plan_asm_rhs<float, double>(B, l, dst);
         plan_asm_rhs<double, double>(B, l, dst);
     }
-    plan_fwd<float>(B, 0, true, dst);
-    plan_fwd<double>(B, 0, true, dst);
-    for (int l = maxpart - 1; l >= 0; --l) {
-        plan_bwd<float, float>(B, l, dst);
-        plan_bwd<float, double>(B, l, dst);
-        plan_bwd<double, double>(B, l, dst);
+    for (bool st : {true, false}) {
+        plan_fwd<float>(B, 0, true, st, dst);
+        plan_fwd<double>(B, 0, true, st, dst);
     }
+    for (int l = maxpart - 1; l >= 0; --l)
+        for (bool st : {true, false}) {
+            plan_bwd<float, float>(B, l, st, dst);
+            plan_bwd<float, double>(B, l, st, dst);
+            plan_bwd<double, double>(B, l, st, dst);
+        }
 }
 
 template <class Tc>
@@ -427,6 +459,7 @@ void plan_vec(Builder &B, int op, std::vector<std::function<Step(char *)>> &dst)
     const int ni = (int)items.size();
     dst.push_back([=](char *base) {
         Step st;
+        st.what = std::string("plan_vec") + " items=" + std::to_string(ni);
         st.run = [=](cudaStream_t s) {
             vec_batch_kernel<Tc><<<ni, 256, 0, s>>>((const VecDesc<Tc> *)(base + od), (const WorkItem *)(base + oi), op);
             count_launch();
@@ -447,18 +480,24 @@ void plan_resid(Builder &B, std::vector<std::function<Step(char *)>> &dst)
         bss_handle *h = b->sys[s];
         if ((h->levels[0].t == F64) != std::is_same<Tr, double>::value) continue;
         const long long per = std::max(1LL, std::min(h->N, 64LL));
-        ResidualDesc<Tr> d{(const double *)h->A, (const double *)h->B, h->x64, (const double *)h->d, (Tr *)h->c0,
-                           h->N, (int)h->n, (int)h->k, per, h->st};
-        const int di = (int)descs.size();
-        descs.push_back(d);
-        smem = std::max(smem, residual_smem_bytes<double>((int)h->n, (int)h->k));
-        for (long long c = 0; c * per < h->N; ++c) items.push_back(WorkItem{di, (int)c});
+        int kc = (int)h->k;  // column chunk whose shared memory fits
+        while (kc > 1 && residual_smem_bytes<double>((int)h->n, kc) > (size_t)200 * 1024) kc = (kc + 1) / 2;
+        for (int j0 = 0; j0 < h->k; j0 += kc) {
+            const int kk = (int)std::min<long long>(kc, h->k - j0);
+            ResidualDesc<Tr> d{(const double *)h->A, (const double *)h->B, h->x64, (const double *)h->d,
+                               (Tr *)h->c0, h->N, (int)h->n, (int)h->k, j0, kk, j0 == 0 ? -1 : 0, per, h->st};
+            const int di = (int)descs.size();
+            descs.push_back(d);
+            smem = std::max(smem, residual_smem_bytes<double>((int)h->n, kk));
+            for (long long c = 0; c * per < h->N; ++c) items.push_back(WorkItem{di, (int)c});
+        }
     }
     if (items.empty()) return;
     const size_t od = put_vec(B.blob, descs), oi = put_vec(B.blob, items);
     const int ni = (int)items.size();
     dst.push_back([=](char *base) {
         Step st;
+        st.what = std::string("plan_resid") + " items=" + std::to_string(ni) + " smem=" + std::to_string(smem);
         st.run = [=](cudaStream_t s) {
             auto kern = residual_batch_kernel<Tr>;
             cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -475,7 +514,7 @@ int run_steps(const std::vector<Step> &steps, cudaStream_t s)
 {
     for (const Step &st : steps) {
         const cudaError_t e = st.run(s);
-        if (e != cudaSuccess) return cuda_fail(e, "batch step");
+        if (e != cudaSuccess) return cuda_fail(e, ("batch step " + st.what).c_str());
     }
     return BSS_OK;
 }
@@ -718,9 +757,10 @@ extern "C" int bss_batch_create(int32_t nsys, const int64_t *N, const int64_t *n
         h->external_arena = true;
         h->kc_max = solve_kc_max((int)n[s], (int)k[s], dtype == BSS_F64 ? 8 : 4);
         if (h->kc_max < k[s] ||
-            (b->mixed && residual_smem_bytes<double>((int)n[s], (int)k[s]) > (size_t)200 * 1024)) {
+            (b->mixed && residual_smem_bytes<double>((int)n[s], 1) > (size_t)200 * 1024)) {
             delete h;
-            rc = fail(BSS_ERR_UNSUPPORTED, "system " + std::to_string(s) + ": k too large for one solve pass");
+            rc = fail(BSS_ERR_UNSUPPORTED,
+                      "system " + std::to_string(s) + ": k too large for one solve pass, or n > 128 in mixed precision");
             break;
         }
         // The plan of a system depends only on its own N and the chain length,

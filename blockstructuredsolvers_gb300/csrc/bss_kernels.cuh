@@ -54,7 +54,7 @@ struct DevStatus {
     int done;
     int iters;        // refinement corrections applied by the last solve
     int need_anorm;   // the next residual also accumulates ||T||_inf
-    int pad;
+    int active;       // batch refinement: this system takes the pending correction
     unsigned long long iters_total;  // corrections over all device-loop solves (never reset)
 };
 
@@ -667,6 +667,326 @@ __global__ void __launch_bounds__(Tile<NB>::THREADS, sizeof(T) == 4 ? 2 : 1)
 }
 
 // ---------------------------------------------------------------------------
+// wide chain factor (n > 64): the recursion step of chain_factor_body with
+// every n x n matrix of the chain in global memory -- the factor outputs
+// V_i, W_i, Y_i are written there anyway, and a partition's working set
+// (a few n x n blocks) stays in L2 -- processed in 64 x 64 tiles staged
+// through shared memory (the Tile<64> products and the 64-wide blocked
+// Cholesky of the fused path).  Per step, with tiles (I, J) of size 64:
+//   S = A_i - W_{i-1}^T W_{i-1}                     (upper tiles, into V_i's slot)
+//   Z = -W_{i-1}^T Y_{i-1}   (first step: B_sL^T)   (into Y_i's slot)
+//   blocked Cholesky S = U^T U: diagonal tile K -> V_KK = U_KK^{-1} (stored in
+//     place), row panel U(K,J) = V_KK^T S(K,J), trailing S(J1,J2) -= U^T U
+//   V = U^{-1} in place: V(I,J) = -V_II sum_{P=I+1..J} U(I,P) V(P,J), columns
+//     right to left, rows bottom-up (so every U read is not yet overwritten)
+//   Y_i = V^T Z, W_i = V^T B_i    in place, row tiles bottom-up (V^T is lower)
+//   S_LL += Y_i^T Y_i
+// Data written in this kernel is read back with ld.global.cg (L2), never
+// through the non-coherent read-only path.
+// ---------------------------------------------------------------------------
+constexpr int WT = 64;  // tile edge of the wide path
+
+__device__ __forceinline__ float ld_cg(const float *p) { return __ldcg(p); }
+__device__ __forceinline__ double ld_cg(const double *p) { return __ldcg(p); }
+
+// tile (I, J) of op(M) (op = transpose or identity) of a column-major n x n
+// matrix into the thread's Tile<64> registers; outside n x n: identity on
+// the diagonal (diag_pad) or zero
+template <class Tg, class T>
+__device__ __forceinline__ void wload(T (&dst)[4][4], const Tg *g, int n, int I, int J, bool diag_pad,
+                                      bool transpose)
+{
+    const int ti = threadIdx.x % 16, tj = threadIdx.x / 16;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int gr = WT * I + ti + 16 * a, gc = WT * J + tj + 16 * b;
+            T v;
+            if (gr < n && gc < n)
+                v = (T)(transpose ? ld_cg(g + gc + (size_t)gr * n) : ld_cg(g + gr + (size_t)gc * n));
+            else
+                v = (diag_pad && gr == gc) ? T(1) : T(0);
+            dst[a][b] = v;
+        }
+}
+
+template <class T>
+__device__ __forceinline__ void wstore(T *g, const T (&src)[4][4], int n, int I, int J, T scale)
+{
+    const int ti = threadIdx.x % 16, tj = threadIdx.x / 16;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int gr = WT * I + ti + 16 * a, gc = WT * J + tj + 16 * b;
+            if (gr < n && gc < n) g[gr + (size_t)gc * n] = scale * src[a][b];
+        }
+}
+
+// acc += sum_{K=k0..k1} op(X)(K, I)^T Y(K, J)  (tiles; op(X) = X^T when tx)
+template <class Tx, class Ty, class T>
+__device__ __forceinline__ void wide_tn(T (&acc)[4][4], const Tx *X, const Ty *Y, int n, int I, int J, int k0,
+                                        int k1, T *sX, T *sY, bool tx)
+{
+    const int ti = threadIdx.x % 16, tj = threadIdx.x / 16;
+    for (int K = k0; K <= k1; ++K) {
+        T r[4][4];
+        wload<Tx, T>(r, X, n, K, I, false, tx);
+        store_tile_smem<T, 64>(sX, r, ti, tj, T(1));
+        wload<Ty, T>(r, Y, n, K, J, false, false);
+        store_tile_smem<T, 64>(sY, r, ti, tj, T(1));
+        __syncthreads();
+        tn_acc<T, 64, TN_FULL>(acc, sX, sY, ti, tj);
+        __syncthreads();
+    }
+}
+
+template <class T>
+constexpr size_t wide_factor_smem()
+{
+    return (size_t)(4 * Geo<T, 64>::SLOT + WT) * sizeof(T) + 16;
+}
+
+constexpr int WIDE_THREADS = 256;
+
+template <class Tin, class T>
+__device__ __noinline__ void wide_chain_factor_body(const ChainFactorArgs<Tin, T> &g, const long long p)
+{
+    constexpr int SLOT = Geo<T, 64>::SLOT;
+    constexpr int LD = Geo<T, 64>::LD;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sX = reinterpret_cast<T *>(smem_raw);
+    T *sY = sX + SLOT;
+    T *sS = sY + SLOT;
+    T *sV = sS + SLOT;
+    T *dinv = sV + SLOT;
+    int *sflag = reinterpret_cast<int *>(dinv + WT);
+    const int tid = threadIdx.x, ti = tid % 16, tj = tid / 16;
+    const int n = g.n;
+    const int NT = (n + WT - 1) / WT;
+    const long long nn = (long long)n * n;
+    const bool seq = g.seq != 0;
+    long long first, last, sL = 0;
+    if (seq) {
+        first = 0;
+        last = g.N - 1;
+    } else {
+        sL = (p * (g.N - 1)) / g.Q;
+        const long long sR = ((p + 1) * (g.N - 1)) / g.Q;
+        first = sL + 1;
+        last = sR - 1;
+    }
+    for (int e = tid; e < SLOT; e += WIDE_THREADS) sV[e] = T(0);  // V_KK's strictly lower panels stay zero
+    __syncthreads();
+
+    for (long long i = first; i <= last; ++i) {
+        const long long t = i - first;
+        const bool has_next = !seq || (i < g.N - 1);
+        T *Vg = g.A_f + i * nn;
+        const Tin *Ag = g.A_in + i * nn;
+        const T *Wp = g.B_f + (i - 1) * nn;  // used when t > 0
+        T *Zg = seq ? nullptr : g.Y + i * nn;
+        const T *Yp = seq ? nullptr : g.Y + (i - 1) * nn;
+
+        // S = A_i - W_{i-1}^T W_{i-1}, upper tiles (every thread rewrites only its own elements)
+        for (int I = 0; I < NT; ++I)
+            for (int J = I; J < NT; ++J) {
+                T acc[4][4];
+                zero_tile<T, 64>(acc);
+                if (t > 0) wide_tn<T, T, T>(acc, Wp, Wp, n, I, J, 0, NT - 1, sX, sY, false);
+                T a[4][4];
+                wload<Tin, T>(a, Ag, n, I, J, I == J, false);
+#pragma unroll
+                for (int x = 0; x < 4; ++x)
+#pragma unroll
+                    for (int y = 0; y < 4; ++y) a[x][y] -= acc[x][y];
+                wstore<T>(Vg, a, n, I, J, T(1));
+            }
+        if (!seq) {
+            if (t > 0) {
+                for (int I = 0; I < NT; ++I)
+                    for (int J = 0; J < NT; ++J) {
+                        T acc[4][4];
+                        zero_tile<T, 64>(acc);
+                        wide_tn<T, T, T>(acc, Wp, Yp, n, I, J, 0, NT - 1, sX, sY, false);
+                        wstore<T>(Zg, acc, n, I, J, T(-1));
+                    }
+            } else {
+                const Tin *Bs = g.B_in + sL * nn;  // Z = B_sL^T
+                for (long long e = tid; e < nn; e += WIDE_THREADS) {
+                    const long long r = e % n, c = e / n;
+                    Zg[e] = (T)Bs[c + r * n];
+                }
+            }
+        }
+        __syncthreads();
+
+        // blocked Cholesky; diagonal tiles end as V_KK, off-diagonal upper tiles as U(K, J)
+        for (int K = 0; K < NT; ++K) {
+            {
+                T a[4][4];
+                wload<T, T>(a, Vg, n, K, K, true, false);
+                store_tile_smem<T, 64>(sS, a, ti, tj, T(1));
+            }
+            __syncthreads();
+            const int bad = chol_inv_blocked<T, 64, WIDE_THREADS>(sS, sV, dinv, sflag, tid);
+            if (bad && tid == 0) record_bad_pivot(g.st, g.level, i);
+            {
+                T v[4][4];
+#pragma unroll
+                for (int x = 0; x < 4; ++x)
+#pragma unroll
+                    for (int y = 0; y < 4; ++y) v[x][y] = sV[(ti + 16 * x) + (tj + 16 * y) * LD];
+                wstore<T>(Vg, v, n, K, K, T(1));
+            }
+            for (int J = K + 1; J < NT; ++J) {
+                T r[4][4];
+                wload<T, T>(r, Vg, n, K, J, false, false);
+                store_tile_smem<T, 64>(sY, r, ti, tj, T(1));
+                __syncthreads();
+                T acc[4][4];
+                zero_tile<T, 64>(acc);
+                tn_acc<T, 64, TN_TRI>(acc, sV, sY, ti, tj);
+                __syncthreads();
+                wstore<T>(Vg, acc, n, K, J, T(1));
+            }
+            __syncthreads();
+            for (int J1 = K + 1; J1 < NT; ++J1)
+                for (int J2 = J1; J2 < NT; ++J2) {
+                    T acc[4][4];
+                    zero_tile<T, 64>(acc);
+                    wide_tn<T, T, T>(acc, Vg, Vg, n, J1, J2, K, K, sX, sY, false);
+                    T s[4][4];
+                    wload<T, T>(s, Vg, n, J1, J2, false, false);
+#pragma unroll
+                    for (int x = 0; x < 4; ++x)
+#pragma unroll
+                        for (int y = 0; y < 4; ++y) s[x][y] -= acc[x][y];
+                    wstore<T>(Vg, s, n, J1, J2, T(1));
+                }
+            __syncthreads();
+        }
+        // V = U^{-1}: off-diagonal tiles in place
+        for (int J = NT - 1; J >= 1; --J)
+            for (int I = J - 1; I >= 0; --I) {
+                T acc[4][4];
+                zero_tile<T, 64>(acc);
+                for (int P = I + 1; P <= J; ++P) {
+                    T r[4][4];
+                    wload<T, T>(r, Vg, n, P, I, false, true);  // U(I, P)^T
+                    store_tile_smem<T, 64>(sX, r, ti, tj, T(1));
+                    wload<T, T>(r, Vg, n, P, J, false, false);  // V(P, J)
+                    store_tile_smem<T, 64>(sY, r, ti, tj, T(1));
+                    __syncthreads();
+                    tn_acc<T, 64, TN_FULL>(acc, sX, sY, ti, tj);
+                    __syncthreads();
+                }
+                store_tile_smem<T, 64>(sY, acc, ti, tj, T(1));
+                {
+                    T r[4][4];
+                    wload<T, T>(r, Vg, n, I, I, false, true);  // V_II^T
+                    store_tile_smem<T, 64>(sX, r, ti, tj, T(1));
+                }
+                __syncthreads();
+                T acc2[4][4];
+                zero_tile<T, 64>(acc2);
+                tn_acc<T, 64, TN_FULL>(acc2, sX, sY, ti, tj);
+                __syncthreads();
+                wstore<T>(Vg, acc2, n, I, J, T(-1));
+                __syncthreads();
+            }
+        for (long long e = tid; e < nn; e += WIDE_THREADS) {  // strictly lower tiles of V are zero
+            const long long r = e % n, c = e / n;
+            if (r / WT > c / WT) Vg[e] = T(0);
+        }
+        __syncthreads();
+
+        // Y_i = V^T Z and W_i = V^T B_i in place, row tiles bottom-up
+        if (!seq)
+            for (int I = NT - 1; I >= 0; --I)
+                for (int J = 0; J < NT; ++J) {
+                    T acc[4][4];
+                    zero_tile<T, 64>(acc);
+                    wide_tn<T, T, T>(acc, Vg, Zg, n, I, J, 0, I, sX, sY, false);
+                    wstore<T>(Zg, acc, n, I, J, T(1));
+                }
+        if (has_next) {
+            const Tin *Bi = g.B_in + i * nn;
+            T *Wg = g.B_f + i * nn;
+            for (int I = NT - 1; I >= 0; --I)
+                for (int J = 0; J < NT; ++J) {
+                    T acc[4][4];
+                    zero_tile<T, 64>(acc);
+                    wide_tn<T, Tin, T>(acc, Vg, Bi, n, I, J, 0, I, sX, sY, false);
+                    wstore<T>(Wg, acc, n, I, J, T(1));
+                }
+        }
+        __syncthreads();
+        if (!seq) {
+            T *Cll = g.C + p * 3 * nn;
+            for (int I = 0; I < NT; ++I)
+                for (int J = 0; J < NT; ++J) {
+                    T acc[4][4];
+                    zero_tile<T, 64>(acc);
+                    wide_tn<T, T, T>(acc, Zg, Zg, n, I, J, 0, NT - 1, sX, sY, false);
+                    if (t > 0) {
+                        T c[4][4];
+                        wload<T, T>(c, Cll, n, I, J, false, false);
+#pragma unroll
+                        for (int x = 0; x < 4; ++x)
+#pragma unroll
+                            for (int y = 0; y < 4; ++y) acc[x][y] += c[x][y];
+                    }
+                    wstore<T>(Cll, acc, n, I, J, T(1));
+                }
+            __syncthreads();
+        }
+    }
+
+    if (!seq) {
+        const T *Wl = g.B_f + last * nn;
+        const T *Yl = g.Y + last * nn;
+        T *Cp = g.C + p * 3 * nn;
+        for (int I = 0; I < NT; ++I)
+            for (int J = 0; J < NT; ++J) {
+                T acc[4][4];
+                zero_tile<T, 64>(acc);
+                wide_tn<T, T, T>(acc, Wl, Wl, n, I, J, 0, NT - 1, sX, sY, false);
+                wstore<T>(Cp + nn, acc, n, I, J, T(1));
+                zero_tile<T, 64>(acc);
+                wide_tn<T, T, T>(acc, Yl, Wl, n, I, J, 0, NT - 1, sX, sY, false);
+                wstore<T>(Cp + 2 * nn, acc, n, I, J, T(1));
+            }
+    }
+}
+
+template <class Tin, class T>
+__global__ void __launch_bounds__(WIDE_THREADS) wide_chain_factor_kernel(ChainFactorArgs<Tin, T> g)
+{
+    wide_chain_factor_body<Tin, T>(g, blockIdx.x);
+}
+
+template <class Tin, class T>
+__global__ void __launch_bounds__(WIDE_THREADS)
+    wide_chain_factor_queue_kernel(const ChainFactorArgs<Tin, T> *__restrict__ descs,
+                                   const WorkItem *__restrict__ items, int nitems, int *head)
+{
+    __shared__ int cur;
+    for (;;) {
+        if (threadIdx.x == 0) cur = atomicAdd(head, 1);
+        __syncthreads();
+        const int it = cur;
+        __syncthreads();
+        if (it >= nitems) break;
+        const WorkItem w = items[it];
+        const ChainFactorArgs<Tin, T> g = descs[w.desc];
+        wide_chain_factor_body<Tin, T>(g, w.p);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // separator system assembly: A'_s = A_{sep s} - S_LL(s) - S_RR(s-1),
 // B'_s = -S_LR(s)     (reference compute_schur_complement!, backbone_cuda.jl:143-157)
 // ---------------------------------------------------------------------------
@@ -821,11 +1141,23 @@ struct SolveArgs {
     int seq;
 };
 
-// shared memory: 2 buffers x 3 blocks + 6 vectors + reduction scratch
+// shared memory: 2 buffers x 3 blocks (staged form only) + 6 vectors +
+// reduction scratch.  Blocks too large to stage (n > 64 in FP64, n > 90 in
+// FP32) are read straight from global memory, once per step, coalesced.
+constexpr size_t SOLVE_SMEM_MAX = 220 * 1024;
+
 template <class T>
-__host__ __device__ constexpr size_t solve_smem_bytes(int n, int kc)
+__host__ __device__ constexpr size_t solve_smem_bytes(int n, int kc, bool staged = true)
 {
-    return (size_t)(6 * n * n + 6 * n * kc + (n * kc > SOLVE_THREADS ? n * kc : SOLVE_THREADS)) * sizeof(T);
+    return (size_t)((staged ? 6 * n * n : 0) + 6 * n * kc + (n * kc > SOLVE_THREADS ? n * kc : SOLVE_THREADS)) *
+           sizeof(T);
+}
+
+// the staged form whenever its double buffer fits for this column chunk
+template <class T>
+__host__ __device__ constexpr bool solve_staged(int n, int kc)
+{
+    return solve_smem_bytes<T>(n, kc, true) <= SOLVE_SMEM_MAX;
 }
 
 template <class T>
@@ -850,14 +1182,14 @@ __device__ __forceinline__ void store_rhs(Tg *__restrict__ g, const T *s, long l
 
 // forward sweep of one partition; for the sequential (coarsest) level the
 // whole chain followed by its backward sweep.
-template <class T>
+template <class T, bool STAGED>
 __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long long p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = g.n, kc = g.kc;
     const int nn = n * n, nkc = n * kc;
-    T *buf = reinterpret_cast<T *>(smem_raw);  // [2][3][nn]: V, W, Y
-    T *srb = buf + 6 * nn;                     // [2][nkc]: RHS block of the step (prefetched)
+    T *buf = reinterpret_cast<T *>(smem_raw);  // [2][3][nn]: V, W, Y (STAGED only)
+    T *srb = buf + (STAGED ? 6 * nn : 0);      // [2][nkc]: RHS block of the step (prefetched)
     T *sy = srb + 2 * nkc;
     T *sbL = sy + nkc;
     T *sbR = sbL + nkc;
@@ -876,8 +1208,10 @@ __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long
     }
     for (int e = threadIdx.x; e < nkc; e += blockDim.x) sbL[e] = T(0);
     // step i uses V_i (slot 0), W_{i-1} (slot 1), Y_i (slot 2) and d_i in buffer (i - first) & 1
-    async_copy(buf, g.Af + first * (long long)nn, nn);
-    if (!seq) async_copy(buf + 2 * nn, g.Y + first * (long long)nn, nn);
+    if (STAGED) {
+        async_copy(buf, g.Af + first * (long long)nn, nn);
+        if (!seq) async_copy(buf + 2 * nn, g.Y + first * (long long)nn, nn);
+    }
     async_copy(srb, rhs_ptr<T>(g.d, first, n, g.k, g.j0), nkc);
     cp_async_commit();
     for (long long i = first; i <= last; ++i) {
@@ -889,25 +1223,30 @@ __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long
         __syncthreads();
         // prefetch step i+1 (W_i is also what bR needs after the last step)
         if (i < last) {
-            async_copy(nxt, g.Af + (i + 1) * (long long)nn, nn);
+            if (STAGED) async_copy(nxt, g.Af + (i + 1) * (long long)nn, nn);
             async_copy(srb + (cb ^ 1) * nkc, rhs_ptr<T>(g.d, i + 1, n, g.k, g.j0), nkc);
         }
-        if (!seq || i < last) async_copy(nxt + nn, g.Bf + i * (long long)nn, nn);
-        if (!seq && i < last) async_copy(nxt + 2 * nn, g.Y + (i + 1) * (long long)nn, nn);
+        if (STAGED && (!seq || i < last)) async_copy(nxt + nn, g.Bf + i * (long long)nn, nn);
+        if (STAGED && !seq && i < last) async_copy(nxt + 2 * nn, g.Y + (i + 1) * (long long)nn, nn);
         cp_async_commit();
+        // matrices of step i: staged in shared memory, or read straight from global memory
+        const T *mV = STAGED ? cur : g.Af + i * (long long)nn;
+        const T *mW = STAGED ? cur + nn : g.Bf + (i - 1) * (long long)nn;
+        const T *mY = STAGED ? cur + 2 * nn : g.Y + i * (long long)nn;
         if (i > first) {
-            cta_tmul(cur + nn, sy, sr, n, kc, T(-1), true);
+            cta_tmul(mW, sy, sr, n, kc, T(-1), true);
             __syncthreads();
         }
-        cta_tmul(cur, sr, sy, n, kc, T(1), false);
+        cta_tmul(mV, sr, sy, n, kc, T(1), false);
         __syncthreads();
-        if (!seq) cta_tmul(cur + 2 * nn, sy, sbL, n, kc, T(1), true);
+        if (!seq) cta_tmul(mY, sy, sbL, n, kc, T(1), true);
         store_rhs(g.d, sy, i, n, g.k, g.j0, kc);
     }
     cp_async_wait_all();
     __syncthreads();
     if (!seq) {
-        const T *wl = buf + (((last + 1 - first) & 1) * 3 + 1) * nn;  // W_last, prefetched in the last step
+        const T *wl = STAGED ? buf + (((last + 1 - first) & 1) * 3 + 1) * nn  // W_last, prefetched in the last step
+                             : g.Bf + last * (long long)nn;
         cta_tmul(wl, sy, sbR, n, kc, T(1), false);
         __syncthreads();
         T *bp = g.bvec + p * 2 * (long long)nkc;
@@ -919,7 +1258,7 @@ __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long
     }
     // sequential level, backward: x_i = V_i (y_i - W_i x_{i+1}); step i uses
     // V_i (slot 0), W_i (slot 1) and y_i
-    async_copy(buf, g.Af + last * (long long)nn, nn);
+    if (STAGED) async_copy(buf, g.Af + last * (long long)nn, nn);
     async_copy(srb, rhs_ptr<T>(g.d, last, n, g.k, g.j0), nkc);
     cp_async_commit();
     for (long long i = last; i >= first; --i) {
@@ -930,29 +1269,33 @@ __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long
         cp_async_wait_all();
         __syncthreads();
         if (i > first) {
-            async_copy(nxt, g.Af + (i - 1) * (long long)nn, nn);
-            async_copy(nxt + nn, g.Bf + (i - 1) * (long long)nn, nn);
+            if (STAGED) {
+                async_copy(nxt, g.Af + (i - 1) * (long long)nn, nn);
+                async_copy(nxt + nn, g.Bf + (i - 1) * (long long)nn, nn);
+            }
             async_copy(srb + (cb ^ 1) * nkc, rhs_ptr<T>(g.d, i - 1, n, g.k, g.j0), nkc);
         }
         cp_async_commit();
+        const T *mV = STAGED ? cur : g.Af + i * (long long)nn;
+        const T *mW = STAGED ? cur + nn : g.Bf + i * (long long)nn;
         if (i < last) {
-            cta_nmul<T>(cur + nn, sx, nullptr, nullptr, sr, sr, T(-1), n, kc, red);
+            cta_nmul<T>(mW, sx, nullptr, nullptr, sr, sr, T(-1), n, kc, red);
             __syncthreads();
         }
-        cta_nmul<T>(cur, sr, nullptr, nullptr, nullptr, sx, T(1), n, kc, red);
+        cta_nmul<T>(mV, sr, nullptr, nullptr, nullptr, sx, T(1), n, kc, red);
         __syncthreads();
         store_rhs(g.d, sx, i, n, g.k, g.j0, kc);
     }
     cp_async_wait_all();
 }
 
-template <class T>
+template <class T, bool STAGED>
 __global__ void __launch_bounds__(SOLVE_THREADS) chain_fwd_kernel(SolveArgs<T> g)
 {
-    chain_fwd_body<T>(g, blockIdx.x);
+    chain_fwd_body<T, STAGED>(g, blockIdx.x);
 }
 
-template <class T>
+template <class T, bool STAGED>
 __global__ void __launch_bounds__(SOLVE_THREADS)
     chain_fwd_queue_kernel(const SolveArgs<T> *__restrict__ descs, const WorkItem *__restrict__ items, int nitems,
                            int *head)
@@ -966,7 +1309,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS)
         if (it >= nitems) break;
         const WorkItem w = items[it];
         const SolveArgs<T> g = descs[w.desc];
-        chain_fwd_body<T>(g, w.p);
+        chain_fwd_body<T, STAGED>(g, w.p);
         __syncthreads();
     }
 }
@@ -995,15 +1338,15 @@ __global__ void assemble_rhs_kernel(const T *__restrict__ d, const T *__restrict
 // x_{last+1} = x_R; also writes x_L (and x_R for the last partition) into
 // the level's separator slots (reference update_boundary! + the scatter
 // gpu_batched.jl:253, and cholesky_solve_batched! :257).
-template <class T, class Tsep>
+template <class T, class Tsep, bool STAGED>
 __device__ __forceinline__ void chain_bwd_body(const SolveArgs<T> &g, const long long p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = g.n, kc = g.kc;
     const int nn = n * n;
     const int nkc = n * kc;
-    T *buf = reinterpret_cast<T *>(smem_raw);  // [2][3][nn]: V_i, W_i, Y_i
-    T *szb = buf + 6 * nn;                     // [2][nkc]: y_i of the step (prefetched)
+    T *buf = reinterpret_cast<T *>(smem_raw);  // [2][3][nn]: V_i, W_i, Y_i (STAGED only)
+    T *szb = buf + (STAGED ? 6 * nn : 0);      // [2][nkc]: y_i of the step (prefetched)
     T *sxL = szb + 2 * nkc;
     T *sxn = sxL + nkc;
     T *sxt = sxn + nkc;
@@ -1012,9 +1355,11 @@ __device__ __forceinline__ void chain_bwd_body(const SolveArgs<T> &g, const long
     const long long sR = ((p + 1) * (g.N - 1)) / g.Q;
     const long long first = sL + 1, last = sR - 1;
     const Tsep *xs = reinterpret_cast<const Tsep *>(g.xsep);
-    async_copy(buf, g.Af + last * (long long)nn, nn);
-    async_copy(buf + nn, g.Bf + last * (long long)nn, nn);
-    async_copy(buf + 2 * nn, g.Y + last * (long long)nn, nn);
+    if (STAGED) {
+        async_copy(buf, g.Af + last * (long long)nn, nn);
+        async_copy(buf + nn, g.Bf + last * (long long)nn, nn);
+        async_copy(buf + 2 * nn, g.Y + last * (long long)nn, nn);
+    }
     async_copy(szb, rhs_ptr<T>(g.d, last, n, g.k, g.j0), nkc);
     cp_async_commit();
     load_rhs(sxL, xs, p, n, g.k, g.j0, kc);
@@ -1030,15 +1375,20 @@ __device__ __forceinline__ void chain_bwd_body(const SolveArgs<T> &g, const long
         cp_async_wait_all();
         __syncthreads();
         if (i > first) {
-            async_copy(nxt, g.Af + (i - 1) * (long long)nn, nn);
-            async_copy(nxt + nn, g.Bf + (i - 1) * (long long)nn, nn);
-            async_copy(nxt + 2 * nn, g.Y + (i - 1) * (long long)nn, nn);
+            if (STAGED) {
+                async_copy(nxt, g.Af + (i - 1) * (long long)nn, nn);
+                async_copy(nxt + nn, g.Bf + (i - 1) * (long long)nn, nn);
+                async_copy(nxt + 2 * nn, g.Y + (i - 1) * (long long)nn, nn);
+            }
             async_copy(szb + (cb ^ 1) * nkc, rhs_ptr<T>(g.d, i - 1, n, g.k, g.j0), nkc);
         }
         cp_async_commit();
-        cta_nmul<T>(cur + 2 * nn, sxL, cur + nn, sxn, sz, sz, T(-1), n, kc, red);
+        const T *mV = STAGED ? cur : g.Af + i * (long long)nn;
+        const T *mW = STAGED ? cur + nn : g.Bf + i * (long long)nn;
+        const T *mY = STAGED ? cur + 2 * nn : g.Y + i * (long long)nn;
+        cta_nmul<T>(mY, sxL, mW, sxn, sz, sz, T(-1), n, kc, red);
         __syncthreads();
-        cta_nmul<T>(cur, sz, nullptr, nullptr, nullptr, sxt, T(1), n, kc, red);
+        cta_nmul<T>(mV, sz, nullptr, nullptr, nullptr, sxt, T(1), n, kc, red);
         __syncthreads();
         for (int e = threadIdx.x; e < n * kc; e += blockDim.x) sxn[e] = sxt[e];
         store_rhs(g.d, sxt, i, n, g.k, g.j0, kc);
@@ -1047,13 +1397,13 @@ __device__ __forceinline__ void chain_bwd_body(const SolveArgs<T> &g, const long
     cp_async_wait_all();
 }
 
-template <class T, class Tsep>
+template <class T, class Tsep, bool STAGED>
 __global__ void __launch_bounds__(SOLVE_THREADS) chain_bwd_kernel(SolveArgs<T> g)
 {
-    chain_bwd_body<T, Tsep>(g, blockIdx.x);
+    chain_bwd_body<T, Tsep, STAGED>(g, blockIdx.x);
 }
 
-template <class T, class Tsep>
+template <class T, class Tsep, bool STAGED>
 __global__ void __launch_bounds__(SOLVE_THREADS)
     chain_bwd_queue_kernel(const SolveArgs<T> *__restrict__ descs, const WorkItem *__restrict__ items, int nitems,
                            int *head)
@@ -1067,7 +1417,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS)
         if (it >= nitems) break;
         const WorkItem w = items[it];
         const SolveArgs<T> g = descs[w.desc];
-        chain_bwd_body<T, Tsep>(g, w.p);
+        chain_bwd_body<T, Tsep, STAGED>(g, w.p);
         __syncthreads();
     }
 }
@@ -1335,6 +1685,8 @@ struct ResidualDesc {
     Tr *r;
     long long N;
     int n, k;
+    int j0, kc;    // column chunk of this descriptor
+    int norm;      // -1: ||T||_inf when the status asks for it (first chunk), 0: never
     long long per_cta;
     DevStatus *st;
 };
@@ -1346,7 +1698,7 @@ __global__ void __launch_bounds__(RES_THREADS, 3) residual_batch_kernel(const Re
     const WorkItem w = items[blockIdx.x];
     const ResidualDesc<Tr> g = descs[w.desc];
     const long long b0 = (long long)w.p * g.per_cta;
-    residual_body<double, Tr>(g.A, g.B, g.x, g.d, g.r, g.N, g.n, g.k, 0, g.k, b0, b0 + g.per_cta, -1, g.st);
+    residual_body<double, Tr>(g.A, g.B, g.x, g.d, g.r, g.N, g.n, g.k, g.j0, g.kc, b0, b0 + g.per_cta, g.norm, g.st);
 }
 
 // one refinement decision on the device (graph mode): relative residual,
@@ -1483,7 +1835,9 @@ __global__ void vec_batch_kernel(const VecDesc<Tc> *__restrict__ descs, const Wo
         case VEC_ABSMAX: m = fmax(m, fabs(g.d[e])); break;
         case VEC_TO_CORR: g.c[e] = (Tc)g.d[e]; break;
         case VEC_SET: g.x[e] = (double)g.c[e]; break;
-        case VEC_ADD: g.x[e] += (double)g.c[e]; break;
+        case VEC_ADD:
+            if (g.st->active) g.x[e] += (double)g.c[e];
+            break;
         default: g.d[e] = g.x[e]; break;
         }
     }
@@ -1513,7 +1867,11 @@ static __global__ void batch_decide_kernel(DevStatus *const *__restrict__ sts, i
     st->need_anorm = 0;
     st->rnorm = 0ULL;
     st->xnorm = 0ULL;
-    if (!done && st->iters < max_refine) {
+    // a system stops taking corrections exactly where it would alone, so its
+    // result does not depend on the other systems of the batch
+    const int cont = (!done && st->iters < max_refine) ? 1 : 0;
+    st->active = cont;
+    if (cont) {
         st->iters += 1;
         st->iters_total += 1;
         atomicOr(any_cont, 1);

@@ -10,10 +10,13 @@
 
 namespace bss {
 
-// largest block size the fused chain kernel handles in one CTA
+// largest block size the fused chain kernel handles in one CTA; larger
+// blocks (up to MAX_WIDE_N) take the wide, tile-streamed path
 constexpr int MAX_FUSED_N = 64;
+constexpr int MAX_WIDE_N = 1024;
+constexpr int WIDE_CLASS = 128;  // tile_for() code of the wide path
 
-int tile_for(int n);  // NB in {16, 32, 64}, or 0 if unsupported
+int tile_for(int n);  // NB in {16, 32, 64}, WIDE_CLASS, or 0 if unsupported
 
 template <class Tin, class T>
 cudaError_t launch_chain_factor(const ChainFactorArgs<Tin, T> &a, cudaStream_t s);

@@ -27,12 +27,26 @@ static cudaError_t chain_factor_nb(const ChainFactorArgs<Tin, T> &a, cudaStream_
 }
 
 template <class Tin, class T>
+static cudaError_t wide_chain_factor(const ChainFactorArgs<Tin, T> &a, cudaStream_t s)
+{
+    const size_t smem = wide_factor_smem<T>();
+    auto kern = wide_chain_factor_kernel<Tin, T>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = a.seq ? 1u : (unsigned)a.Q;
+    kern<<<grid, WIDE_THREADS, smem, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class Tin, class T>
 cudaError_t launch_chain_factor(const ChainFactorArgs<Tin, T> &a, cudaStream_t s)
 {
     switch (tile_for(a.n)) {
     case 16: return chain_factor_nb<Tin, T, 16>(a, s);
     case 32: return chain_factor_nb<Tin, T, 32>(a, s);
     case 64: return chain_factor_nb<Tin, T, 64>(a, s);
+    case WIDE_CLASS: return wide_chain_factor<Tin, T>(a, s);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -49,12 +63,24 @@ static int ctas_nb()
 }
 
 template <class Tin, class T>
+static int wide_ctas()
+{
+    const size_t smem = wide_factor_smem<T>();
+    auto kern = wide_chain_factor_kernel<Tin, T>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
+    int nblk = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, kern, WIDE_THREADS, smem) != cudaSuccess) return 1;
+    return nblk > 0 ? nblk : 1;
+}
+
+template <class Tin, class T>
 int chain_factor_ctas_per_sm(int n)
 {
     switch (tile_for(n)) {
     case 16: return ctas_nb<Tin, T, 16>();
     case 32: return ctas_nb<Tin, T, 32>();
     case 64: return ctas_nb<Tin, T, 64>();
+    case WIDE_CLASS: return wide_ctas<Tin, T>();
     default: return 1;
     }
 }
@@ -78,8 +104,9 @@ static cudaError_t set_solve_smem(const void *kern, size_t smem)
 template <class T>
 cudaError_t launch_chain_fwd(const SolveArgs<T> &a, cudaStream_t s)
 {
-    const size_t smem = solve_smem_bytes<T>(a.n, a.kc);
-    auto kern = chain_fwd_kernel<T>;
+    const bool staged = solve_staged<T>(a.n, a.kc);
+    const size_t smem = solve_smem_bytes<T>(a.n, a.kc, staged);
+    auto kern = staged ? chain_fwd_kernel<T, true> : chain_fwd_kernel<T, false>;
     cudaError_t e = set_solve_smem<T>((const void *)kern, smem);
     if (e != cudaSuccess) return e;
     const unsigned grid = a.seq ? 1u : (unsigned)a.Q;
@@ -91,8 +118,9 @@ cudaError_t launch_chain_fwd(const SolveArgs<T> &a, cudaStream_t s)
 template <class T, class Tsep>
 cudaError_t launch_chain_bwd(const SolveArgs<T> &a, cudaStream_t s)
 {
-    const size_t smem = solve_smem_bytes<T>(a.n, a.kc);
-    auto kern = chain_bwd_kernel<T, Tsep>;
+    const bool staged = solve_staged<T>(a.n, a.kc);
+    const size_t smem = solve_smem_bytes<T>(a.n, a.kc, staged);
+    auto kern = staged ? chain_bwd_kernel<T, Tsep, true> : chain_bwd_kernel<T, Tsep, false>;
     cudaError_t e = set_solve_smem<T>((const void *)kern, smem);
     if (e != cudaSuccess) return e;
     kern<<<(unsigned)a.Q, SOLVE_THREADS, smem, s>>>(a);

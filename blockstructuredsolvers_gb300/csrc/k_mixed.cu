@@ -45,18 +45,22 @@ int tile_for(int n)
     if (n <= 16) return 16;
     if (n <= 32) return 32;
     if (n <= 64) return 64;
+    if (n <= MAX_WIDE_N) return WIDE_CLASS;
     return 0;
 }
 
 int solve_kc_max(int n, int k, int elem_bytes)
 {
-    // largest column chunk whose double-buffered solve kernels fit in shared memory
-    const long long budget = 220LL * 1024 / elem_bytes;
+    // largest column chunk (<= 32) whose solve kernels fit in shared memory:
+    // in the staged form when that fits for one column, else reading the
+    // blocks from global memory (the launch picks the staged form whenever
+    // it fits the chunk, for levels of either precision)
+    const bool staged = elem_bytes == 8 ? solve_staged<double>(n, 1) : solve_staged<float>(n, 1);
     int best = 1;
     for (int kc = 1; kc <= 32 && kc <= k; ++kc) {
-        const long long nk = (long long)n * kc;
-        const long long need = 6LL * n * n + 5 * nk + (nk > SOLVE_THREADS ? nk : SOLVE_THREADS);
-        if (need > budget) break;
+        const size_t need = elem_bytes == 8 ? solve_smem_bytes<double>(n, kc, staged)
+                                            : solve_smem_bytes<float>(n, kc, staged);
+        if (need > SOLVE_SMEM_MAX) break;
         best = kc;
     }
     return best;

@@ -160,7 +160,7 @@ def test_batch_not_spd_reports_system(bss):
 def test_batch_rejects_unsupported_block_size(bss):
     import torch
     with pytest.raises(bss.BSSError):
-        bss.initialize_multi([10, 10], [16, 200], [1, 1], torch.float64)
+        bss.initialize_multi([10, 10], [16, 2000], [1, 1], torch.float64)
 
 
 def test_batch_cfg3_family_sample(bss):
