@@ -387,6 +387,138 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+# --------------------------------------------------------------------------
+# served Kalman-smoother request stream (config 4)
+# --------------------------------------------------------------------------
+KF_SIZES = (8, 16, 32, 64)
+
+
+def gen_kf_stream(n_requests, rate, repeat_frac=0.3, seed=4, recent=32):
+    """Seeded request stream: Poisson arrivals at `rate` req/s; a request is
+    a new Kalman model (n from {8,16,32,64}, horizon N ~ U{50..5000}, F ~
+    N(0,1) rescaled to spectral radius 0.95, H ~ N(0,1) (n/2 x n), Q = 0.1 I,
+    R = 0.5 I, observations simulated from the model) or, with probability
+    `repeat_frac`, new observations for one of the `recent` last models
+    (a repeat right-hand side on its resident factor).  Host buffers are
+    page-locked torch tensors in column-major storage order."""
+    import numpy as np
+    import torch
+    pin = (lambda t: t.pin_memory()) if torch.cuda.is_available() else (lambda t: t)
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, n_requests) if rate else np.zeros(n_requests)
+    t_arr = np.cumsum(gaps) - gaps[0]
+    kinds = []
+    models = []
+    for i in range(n_requests):
+        if models and rng.random() < repeat_frac:
+            kinds.append(("rhs", int(rng.integers(max(0, len(models) - recent), len(models)))))
+        else:
+            n = int(rng.choice(KF_SIZES))
+            N = int(rng.integers(50, 5001))
+            models.append({"n": n, "N": N})
+            kinds.append(("new", len(models) - 1))
+    # models, batched per state size
+    for n in KF_SIZES:
+        idx = [j for j, mdl in enumerate(models) if mdl["n"] == n]
+        if not idx:
+            continue
+        m = n // 2
+        F = rng.standard_normal((len(idx), n, n))
+        rho = np.abs(np.linalg.eigvals(F)).max(axis=1)
+        F *= (0.95 / rho)[:, None, None]
+        H = rng.standard_normal((len(idx), m, n))
+        for j, a in enumerate(idx):
+            models[a]["F"], models[a]["H"] = F[j], H[j]
+    # observation sequences, one per request (new models and repeats),
+    # simulated for all requests of one state size at once
+    Ys = [None] * n_requests
+    for n in KF_SIZES:
+        idx = [i for i, (kind, a) in enumerate(kinds) if models[a]["n"] == n]
+        if not idx:
+            continue
+        m = n // 2
+        Fb = np.stack([models[kinds[i][1]]["F"] for i in idx])
+        Hb = np.stack([models[kinds[i][1]]["H"] for i in idx])
+        Ns = np.array([models[kinds[i][1]]["N"] for i in idx])
+        T = int(Ns.max())
+        W = rng.standard_normal((T, len(idx), n)) * np.sqrt(0.1)
+        V = rng.standard_normal((len(idx), T, m)) * np.sqrt(0.5)
+        dev = "cuda" if torch.cuda.is_available() else "cpu"  # input synthesis only
+        Ft, Wt = torch.from_numpy(Fb).to(dev), torch.from_numpy(W).to(dev)
+        Xt = torch.empty((T, len(idx), n), dtype=torch.float64, device=dev)
+        x = torch.zeros((len(idx), n, 1), dtype=torch.float64, device=dev)
+        for t in range(T):
+            x = torch.bmm(Ft, x) + Wt[t][:, :, None]
+            Xt[t] = x[:, :, 0]
+        X = Xt.permute(1, 0, 2).cpu().numpy()
+        Y = np.matmul(X, np.swapaxes(Hb, 1, 2)) + V
+        for j, i in enumerate(idx):
+            Ys[i] = pin(torch.from_numpy(np.ascontiguousarray(Y[j, :Ns[j]])).reshape(int(Ns[j]), 1, m))
+    reqs = []
+    for i, ((kind, a), t) in enumerate(zip(kinds, t_arr)):
+        mdl = models[a]
+        reqs.append({"kind": kind, "model": a, "t": float(t), "y": Ys[i],
+                     "x": pin(torch.zeros((mdl["N"], 1, mdl["n"]), dtype=torch.float64))})
+    for mdl in models:
+        n, m = mdl["n"], mdl["n"] // 2
+        colmaj = lambda M: pin(torch.from_numpy(np.ascontiguousarray(M.T)))
+        mdl["Fh"], mdl["Hh"] = colmaj(mdl["F"]), colmaj(mdl["H"])
+        mdl["Qi"] = pin(torch.eye(n, dtype=torch.float64).mul_(10.0))
+        mdl["Ri"] = pin(torch.eye(m, dtype=torch.float64).mul_(2.0))
+    return models, reqs
+
+
+def run_served(bss, precision, models, reqs, budget=100 * 10**9, streams=8):
+    """Replay the stream against a server: a submitter thread releases each
+    request at its arrival time; returns solves/s, latency percentiles and
+    the worst relative residual the solver reported."""
+    import threading
+    srv = bss.Server(hbm_budget_bytes=budget, streams=streams, max_inflight=64, precision=precision)
+    fids = {}
+    ids = [None] * len(reqs)
+    errors = []
+
+    def submitter():
+        t0 = time.perf_counter()
+        for i, r in enumerate(reqs):
+            wait = r["t"] - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            mdl = models[r["model"]]
+            try:
+                if r["kind"] == "new":
+                    rid, fid = srv.submit_kalman(mdl["Fh"], mdl["Hh"], mdl["Qi"], mdl["Ri"], r["y"], r["x"],
+                                                 keep=True)
+                    fids[r["model"]] = fid
+                else:
+                    rid = srv.submit_rhs(fids[r["model"]], r["y"], r["x"])
+                ids[i] = rid
+            except Exception as e:  # an evicted factor: counted, not fatal
+                errors.append(str(e))
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    th.join()
+    worst = 0.0
+    steps = []
+    failed = 0
+    for rid in ids:
+        if rid is None:
+            continue
+        info = srv.wait(rid, check=False)
+        if info["status"] != 0:
+            failed += 1
+        worst = max(worst, info["rel_residual"])
+        steps.append(info["refine_steps"])
+    st = srv.stats()
+    srv.close()
+    return {"solves_per_s": st["completed"] / st["busy_s"] if st["busy_s"] > 0 else None,
+            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
+            "completed": st["completed"], "failed": failed + len(errors), "evictions": st["evictions"],
+            "bytes_peak": st["bytes_peak"], "worst_rel_residual": worst if precision == "mixed" else None,
+            "mean_refine_steps": (sum(steps) / len(steps)) if steps else None}
+
+
 def roofline_chain_factor(bss, A, B, d, hbm_gbs, peak_kind):
     """Roofline of the dominant kernel of the mixed path: the level-0 chain
     factor kernel (FP64 A_i, B_i in; FP32 V_i, W_i, Y_i out).  Algorithmic

@@ -26,7 +26,7 @@ from ._lib import BSSError, NotSPDError  # noqa: F401
 __all__ = [
     "BlockTriDiagData_batched", "BlockTriDiagData_seq", "initialize_batched", "initialize_seq",
     "factorize_", "solve_", "factorize", "solve", "synchronize", "get_info", "residual",
-    "plan_reference", "BSSError", "NotSPDError", "MultiSystemBatch", "initialize_multi",
+    "plan_reference", "BSSError", "NotSPDError", "MultiSystemBatch", "initialize_multi", "Server", "kf_build",
 ]
 
 
@@ -339,6 +339,132 @@ def initialize_multi(Ns, ns, ks=None, T=None, *, precision: str = "plain", max_r
 
 def plan_reference(N: int):
     return _lib.plan_reference(N)
+
+
+def _ptr(a):
+    """Address of a host buffer: a C-contiguous float64 numpy array or a CPU
+    torch tensor (page-locked ones make the server's copies asynchronous)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        if a.dtype != _torch().float64 or not a.is_contiguous():
+            raise ValueError("host tensors must be contiguous float64")
+        return ctypes.c_void_p(a.data_ptr())
+    import numpy as np
+    if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("host arrays must be C-contiguous float64")
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def kf_build(F, H, Qinv, Rinv, y, A_out, B_out, d_out, P0inv=None, x0=None, stream=None) -> None:
+    """Kalman-smoother normal equations on the device (build_kf_blocks,
+    benchmark/benchmark_kf.jl:105-154): column-major CUDA float64 tensors
+    F (n,n), H (m,n), Qinv (n,n), Rinv (m,m), y (m,k,N) -> A (n,n,N),
+    B (n,n,N-1), d (n,k,N)."""
+    m, k, N = y.shape
+    n = F.shape[0]
+    dp = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
+    _lib.check(_lib.load().bss_kf_build(N, n, m, k, dp(F), dp(H), dp(Qinv), dp(Rinv), dp(P0inv), dp(x0), dp(y),
+                                        dp(A_out), dp(B_out) if N > 1 else None, dp(d_out), _stream_ptr(stream)))
+
+
+class Server:
+    """Request server over the C ABI (bss_server_*): continuous batching of
+    independent solves under an HBM budget, resident factors for repeat
+    right-hand sides, p50/p99 latency.  Host buffers (inputs and outputs)
+    must stay alive and unchanged until ``wait`` returns for the request;
+    this class keeps references to them until then."""
+
+    def __init__(self, hbm_budget_bytes=None, streams=None, max_inflight=None, precision="mixed",
+                 max_refine=None, tol=None):
+        L = _lib.load()
+        o = _lib.ServerOptions()
+        L.bss_server_default_options(ctypes.byref(o))
+        if hbm_budget_bytes is not None:
+            o.hbm_budget_bytes = int(hbm_budget_bytes)
+        if streams is not None:
+            o.streams = int(streams)
+        if max_inflight is not None:
+            o.max_inflight = int(max_inflight)
+        o.precision = {"plain": _lib.BSS_PRECISION_PLAIN, "mixed": _lib.BSS_PRECISION_MIXED}[precision]
+        if max_refine is not None:
+            o.max_refine = int(max_refine)
+        if tol is not None:
+            o.tol = float(tol)
+        _torch().cuda.current_device()
+        h = ctypes.c_void_p()
+        _lib.check(L.bss_server_create(ctypes.byref(o), ctypes.byref(h)))
+        self._h = h.value
+        self._keep = {}
+
+    def close(self):
+        if self._h:
+            _lib.load().bss_server_destroy(self._h)
+            self._h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, A, B, d, x_out, keep=False):
+        """A (N,n,n) storage order (block i column-major = numpy (N, c, r)),
+        B (N-1,n,n), d (N,k,n) -> x_out (N,k,n).  Returns (request, factor)."""
+        N, n = A.shape[0], A.shape[1]
+        k = d.shape[1]
+        rid, fid = ctypes.c_uint64(), ctypes.c_uint64()
+        _lib.check(_lib.load().bss_server_submit(self._h, N, n, k, _ptr(A), _ptr(B) if N > 1 else None, _ptr(d),
+                                                 1 if keep else 0, _ptr(x_out), ctypes.byref(rid),
+                                                 ctypes.byref(fid)))
+        self._keep[rid.value] = (A, B, d, x_out)
+        return rid.value, fid.value
+
+    def submit_kalman(self, F, H, Qinv, Rinv, y, x_out, P0inv=None, x0=None, keep=False):
+        """Column-major host arrays: F (n,n) as numpy (c, r), H (m,n) as (n, m),
+        Qinv, Rinv, y (m,k,N) as numpy (N, k, m) -> x_out (N, k, n)."""
+        N, k, m = y.shape
+        n = F.shape[0]
+        rid, fid = ctypes.c_uint64(), ctypes.c_uint64()
+        _lib.check(_lib.load().bss_server_submit_kalman(self._h, N, n, m, k, _ptr(F), _ptr(H), _ptr(Qinv),
+                                                        _ptr(Rinv), _ptr(P0inv), _ptr(x0), _ptr(y),
+                                                        1 if keep else 0, _ptr(x_out), ctypes.byref(rid),
+                                                        ctypes.byref(fid)))
+        self._keep[rid.value] = (F, H, Qinv, Rinv, P0inv, x0, y, x_out)
+        return rid.value, fid.value
+
+    def submit_rhs(self, factor_id, d_or_y, x_out):
+        rid = ctypes.c_uint64()
+        _lib.check(_lib.load().bss_server_submit_rhs(self._h, int(factor_id), _ptr(d_or_y), _ptr(x_out),
+                                                     ctypes.byref(rid)))
+        self._keep[rid.value] = (d_or_y, x_out)
+        return rid.value
+
+    def wait(self, request_id, check=True) -> dict:
+        inf = _lib.RequestInfo()
+        rc = _lib.load().bss_server_wait(self._h, int(request_id), ctypes.byref(inf))
+        self._keep.pop(int(request_id), None)
+        out = {k: getattr(inf, k) for k, _ in _lib.RequestInfo._fields_}
+        if check:
+            _lib.check(rc)
+        return out
+
+    def poll(self, request_id) -> bool:
+        done = ctypes.c_int32()
+        _lib.check(_lib.load().bss_server_poll(self._h, int(request_id), ctypes.byref(done)))
+        return bool(done.value)
+
+    def release(self, factor_id) -> None:
+        _lib.check(_lib.load().bss_server_release(self._h, int(factor_id)))
+
+    def stats(self) -> dict:
+        st = _lib.ServerStats()
+        _lib.check(_lib.load().bss_server_get_stats(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in _lib.ServerStats._fields_}
+
+    def reset_stats(self) -> None:
+        _lib.check(_lib.load().bss_server_reset_stats(self._h))
 
 
 def colmajor_empty(shape, dtype, device="cuda"):

@@ -38,6 +38,9 @@ EXPORTS = (
     "bss_factorize_levels", "bss_get_level", "bss_factor_solve_noalloc", "bss_kernel_launches",
     "bss_version", "bss_batch_create", "bss_batch_destroy", "bss_batch_get_tensors", "bss_batch_get_dims",
     "bss_batch_factorize", "bss_batch_solve", "bss_batch_synchronize", "bss_batch_get_info",
+    "bss_kf_build", "bss_server_default_options", "bss_server_create", "bss_server_destroy", "bss_server_submit",
+    "bss_server_submit_kalman", "bss_server_submit_rhs", "bss_server_wait", "bss_server_poll",
+    "bss_server_release", "bss_server_get_stats", "bss_server_reset_stats",
 )
 
 
@@ -51,6 +54,45 @@ class Options(ctypes.Structure):
         ("use_graphs", ctypes.c_int32),
         ("tol", ctypes.c_double),
         ("chain_blocks", ctypes.c_int32),
+    ]
+
+
+class ServerOptions(ctypes.Structure):
+    _fields_ = [
+        ("hbm_budget_bytes", ctypes.c_int64),
+        ("streams", ctypes.c_int32),
+        ("max_inflight", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("max_refine", ctypes.c_int32),
+        ("tol", ctypes.c_double),
+    ]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int32),
+        ("refine_steps", ctypes.c_int32),
+        ("rel_residual", ctypes.c_double),
+        ("latency_ms", ctypes.c_double),
+        ("queue_ms", ctypes.c_double),
+        ("factor_id", ctypes.c_uint64),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_int64),
+        ("completed", ctypes.c_int64),
+        ("failed", ctypes.c_int64),
+        ("evictions", ctypes.c_int64),
+        ("resident_factors", ctypes.c_int64),
+        ("bytes_in_use", ctypes.c_int64),
+        ("bytes_peak", ctypes.c_int64),
+        ("p50_ms", ctypes.c_double),
+        ("p99_ms", ctypes.c_double),
+        ("mean_ms", ctypes.c_double),
+        ("max_ms", ctypes.c_double),
+        ("busy_s", ctypes.c_double),
     ]
 
 
@@ -123,8 +165,24 @@ def load(path: str | None = None):
     L.bss_batch_solve.argtypes = [vp]
     L.bss_batch_synchronize.argtypes = [vp]
     L.bss_batch_get_info.argtypes = [vp, i32, ctypes.POINTER(Info)]
+    L.bss_kf_build.argtypes = [i64, i64, i64, i64] + [vp] * 10 + [vp]
+    L.bss_server_default_options.argtypes = [ctypes.POINTER(ServerOptions)]
+    L.bss_server_default_options.restype = None
+    u64 = ctypes.c_uint64
+    pu64 = ctypes.POINTER(u64)
+    L.bss_server_create.argtypes = [ctypes.POINTER(ServerOptions), ctypes.POINTER(vp)]
+    L.bss_server_destroy.argtypes = [vp]
+    L.bss_server_submit.argtypes = [vp, i64, i64, i64, vp, vp, vp, i32, vp, pu64, pu64]
+    L.bss_server_submit_kalman.argtypes = [vp, i64, i64, i64, i64, vp, vp, vp, vp, vp, vp, vp, i32, vp, pu64, pu64]
+    L.bss_server_submit_rhs.argtypes = [vp, u64, vp, vp, pu64]
+    L.bss_server_wait.argtypes = [vp, u64, ctypes.POINTER(RequestInfo)]
+    L.bss_server_poll.argtypes = [vp, u64, ctypes.POINTER(i32)]
+    L.bss_server_release.argtypes = [vp, u64]
+    L.bss_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+    L.bss_server_reset_stats.argtypes = [vp]
     for name in EXPORTS:
-        if name not in ("bss_default_options", "bss_last_error_string", "bss_version", "bss_kernel_launches"):
+        if name not in ("bss_default_options", "bss_last_error_string", "bss_version", "bss_kernel_launches",
+                        "bss_server_default_options"):
             getattr(L, name).restype = ctypes.c_int
     if path is None:
         _lib = L

@@ -711,58 +711,103 @@ int chain_solve(bss_handle *h)
     return BSS_OK;
 }
 
-int solve_mixed(bss_handle *h)
+}  // namespace
+
+// Mixed solve in asynchronous pieces: each enqueues its work on h->ls and
+// ends with the status (relative residual, convergence) copied to the pinned
+// h->h_st, so a driver can wait on an event instead of the stream and
+// interleave many systems (the request server does).
+//   begin:   c0 = d; x = A32^{-1} c0; r = d - T x; relres
+//   correct: c0 = A32^{-1} r; x += c0; r = d - T x; relres
+//   finish:  d = x
+namespace {
+
+int residual_check(bss_handle *h)
+{
+    const double *d64 = (const double *)h->d;
+    DevStatus *st = h->st;
+    BSS_CUDA(cudaMemsetAsync(&st->rnorm, 0, 2 * sizeof(unsigned long long), h->ls));
+    const int wn = h->need_anorm ? 1 : 0;
+    h->need_anorm = false;
+    if (wn) BSS_CUDA(cudaMemsetAsync(&st->need_anorm, 0, sizeof(int), h->ls));
+    if (h->levels[0].t == F32)
+        BSS_CUDA((launch_residual<double, float>((const double *)h->A, (const double *)h->B, h->x64, d64,
+                                                 (float *)h->c0, h->N, (int)h->n, (int)h->k, wn, st, h->ls)));
+    else
+        BSS_CUDA((launch_residual<double, double>((const double *)h->A, (const double *)h->B, h->x64, d64,
+                                                  (double *)h->c0, h->N, (int)h->n, (int)h->k, wn, st, h->ls)));
+    BSS_CUDA(launch_relres(st, h->opt.tol, h->ls));
+    BSS_CUDA(cudaMemcpyAsync(h->h_st, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->ls));
+    return BSS_OK;
+}
+
+int chain_solve(bss_handle *h);
+
+}  // namespace
+
+int bss::mixed_begin(bss_handle *h)
 {
     const long long cnt = h->N * h->n * h->k;
     const double *d64 = (const double *)h->d;
-    const bool c_is_f32 = h->levels[0].t == F32;
-    DevStatus *st = h->st;
-    BSS_CUDA(cudaMemsetAsync(&st->dnorm, 0, sizeof(unsigned long long), h->ls));
-    BSS_CUDA(launch_absmax<double>(d64, cnt, &st->dnorm, h->ls));
-    if (c_is_f32)
+    BSS_CUDA(cudaMemsetAsync(&h->st->dnorm, 0, sizeof(unsigned long long), h->ls));
+    BSS_CUDA(launch_absmax<double>(d64, cnt, &h->st->dnorm, h->ls));
+    if (h->levels[0].t == F32)
         BSS_CUDA((launch_convert<double, float>((float *)h->c0, d64, cnt, h->ls)));
     else
         BSS_CUDA((launch_convert<double, double>((double *)h->c0, d64, cnt, h->ls)));
     int rc = chain_solve(h);
     if (rc) return rc;
-    if (c_is_f32)
+    if (h->levels[0].t == F32)
         BSS_CUDA(launch_update<float>(h->x64, (const float *)h->c0, cnt, 1, h->ls));
     else
         BSS_CUDA(launch_update<double>(h->x64, (const double *)h->c0, cnt, 1, h->ls));
+    return residual_check(h);
+}
+
+int bss::mixed_correct(bss_handle *h)
+{
+    const long long cnt = h->N * h->n * h->k;
+    int rc = chain_solve(h);
+    if (rc) return rc;
+    if (h->levels[0].t == F32)
+        BSS_CUDA(launch_update<float>(h->x64, (const float *)h->c0, cnt, 0, h->ls));
+    else
+        BSS_CUDA(launch_update<double>(h->x64, (const double *)h->c0, cnt, 0, h->ls));
+    return residual_check(h);
+}
+
+int bss::mixed_finish(bss_handle *h)
+{
+    const long long cnt = h->N * h->n * h->k;
+    BSS_CUDA(cudaMemcpyAsync(h->d, h->x64, cnt * sizeof(double), cudaMemcpyDeviceToDevice, h->ls));
+    return BSS_OK;
+}
+
+namespace {
+
+// eager mixed solve: the host waits for the status after every step
+int solve_mixed(bss_handle *h)
+{
+    int rc = mixed_begin(h);
+    if (rc) return rc;
+    BSS_CUDA(cudaStreamSynchronize(h->ls));
     int steps = 0;
     bool converged = false;
-    for (int it = 0; it <= h->opt.max_refine; ++it) {
-        BSS_CUDA(cudaMemsetAsync(&st->rnorm, 0, 2 * sizeof(unsigned long long), h->ls));
-        const int wn = h->need_anorm ? 1 : 0;
-        h->need_anorm = false;
-        if (wn) BSS_CUDA(cudaMemsetAsync(&st->need_anorm, 0, sizeof(int), h->ls));
-        if (c_is_f32)
-            BSS_CUDA((launch_residual<double, float>((const double *)h->A, (const double *)h->B, h->x64, d64,
-                                                     (float *)h->c0, h->N, (int)h->n, (int)h->k, wn, st,
-                                                     h->ls)));
-        else
-            BSS_CUDA((launch_residual<double, double>((const double *)h->A, (const double *)h->B, h->x64, d64,
-                                                      (double *)h->c0, h->N, (int)h->n, (int)h->k, wn, st,
-                                                      h->ls)));
-        BSS_CUDA(launch_relres(st, h->opt.tol, h->ls));
-        BSS_CUDA(cudaMemcpyAsync(h->h_st, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->ls));
-        BSS_CUDA(cudaStreamSynchronize(h->ls));
+    for (;;) {
         h->info.rel_residual = h->h_st->relres;
         if (h->h_st->done) {
             converged = true;
             break;
         }
-        if (it == h->opt.max_refine) break;
-        rc = chain_solve(h);
+        if (steps == h->opt.max_refine) break;
+        rc = mixed_correct(h);
         if (rc) return rc;
-        if (c_is_f32)
-            BSS_CUDA(launch_update<float>(h->x64, (const float *)h->c0, cnt, 0, h->ls));
-        else
-            BSS_CUDA(launch_update<double>(h->x64, (const double *)h->c0, cnt, 0, h->ls));
+        BSS_CUDA(cudaStreamSynchronize(h->ls));
         ++steps;
     }
     h->info.refine_steps = steps;
-    BSS_CUDA(cudaMemcpyAsync(h->d, h->x64, cnt * sizeof(double), cudaMemcpyDeviceToDevice, h->ls));
+    rc = mixed_finish(h);
+    if (rc) return rc;
     if (!converged) h->sticky = BSS_ERR_NOT_CONVERGED;
     return BSS_OK;
 }

@@ -96,4 +96,10 @@ ChainFactorArgs<Tin, T> make_factor_args(bss_handle *h, int l);
 template <class T>
 SolveArgs<T> make_solve_args(bss_handle *h, int l, int j0, int kc);
 
+// asynchronous pieces of the mixed-precision solve (enqueue on h->ls; each
+// of begin/correct ends with the status copied to the pinned h->h_st)
+int mixed_begin(bss_handle *h);
+int mixed_correct(bss_handle *h);
+int mixed_finish(bss_handle *h);
+
 }  // namespace bss

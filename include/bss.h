@@ -205,6 +205,100 @@ int bss_batch_solve(bss_batch *b);
 int bss_batch_synchronize(bss_batch *b);
 int bss_batch_get_info(bss_batch *b, int32_t sys, bss_info *info);
 
+/* ---- Kalman-smoother blocks built on the device ------------------------------
+ * Replaces build_kf_blocks (reference benchmark/benchmark_kf.jl:105-154),
+ * which assembles the normal equations of a linear-Gaussian state-space
+ * model on the host.  All pointers are DEVICE memory, column-major, FP64:
+ *   F (n x n), H (m x n), Qinv (n x n) = Q^{-1}, Rinv (m x m) = R^{-1},
+ *   P0inv (n x n) or NULL, x0 (n) or NULL, y (m x k x N): k observation
+ *   sequences (the reference has k = 1).
+ * Output A (n x n x N), B (n x n x (N-1)), d (n x k x N):
+ *   B_i = -F^T Q^{-1};  d_i = H^T R^{-1} y_i  (+ P0^{-1} x0 at i = 0)
+ *   with P0inv: A_0 = H^T R^{-1} H + P0^{-1} + F^T Q^{-1} F,
+ *               A_{N-1} = H^T R^{-1} H + Q^{-1}, the others
+ *               H^T R^{-1} H + Q^{-1} + F^T Q^{-1} F   (the reference's form);
+ *   P0inv NULL: every A_i = H^T R^{-1} H + Q^{-1} + F^T Q^{-1} F.
+ * A_i is symmetrised from its upper triangle (the reference's
+ * Symmetric(Akk)).  Asynchronous on `stream`. */
+int bss_kf_build(int64_t N, int64_t n, int64_t m, int64_t k, const double *F, const double *H, const double *Qinv,
+                 const double *Rinv, const double *P0inv, const double *x0, const double *y, double *A, double *B,
+                 double *d, void *stream);
+
+/* ---- request server: continuous batching under an HBM budget ------------------
+ * No counterpart in the reference.  A worker thread owns the GPU work:
+ * requests are admitted as streams and memory free up (FIFO on memory; a
+ * request larger than the whole budget fails with BSS_ERR_OOM), each runs on
+ * one of `streams` CUDA streams so the work of concurrent requests overlaps
+ * on the device, and the mixed-precision refinement loop of every request
+ * advances on completion events (no host thread blocks on a stream).  Each
+ * request's system gets its own plan and workspace, so its result is the
+ * same alone and in any mix.  Factors of requests submitted with `keep`
+ * stay resident for repeat right-hand sides until released, or until the
+ * budget needs their memory (least recently used first; an RHS request on
+ * an evicted factor fails with BSS_ERR_STATE, at submit or, if the factor
+ * was evicted while the request queued, in its result).
+ * Host buffers passed to submit calls (inputs and x_out) must stay valid and
+ * unchanged until bss_server_wait returns for that request; page-locked
+ * buffers make the copies asynchronous.  All tensors are FP64, column-major
+ * as above; x_out receives x (n x k x N). */
+typedef struct bss_server bss_server;
+
+typedef struct {
+    int64_t hbm_budget_bytes;  /* device memory for all requests (default 100 GB)  */
+    int32_t streams;           /* concurrent CUDA streams (default 8)               */
+    int32_t max_inflight;      /* requests on the GPU at once (default 64)          */
+    int32_t precision;         /* BSS_PRECISION_MIXED (default) or _PLAIN (FP64)    */
+    int32_t max_refine;        /* default 10                                        */
+    double tol;                /* default 1e-12                                     */
+} bss_server_options;
+
+typedef struct {
+    int32_t status;        /* BSS_OK, BSS_ERR_NOT_SPD, BSS_ERR_NOT_CONVERGED, ...   */
+    int32_t refine_steps;
+    double rel_residual;   /* mixed: relative residual of x; -1 in plain precision  */
+    double latency_ms;     /* submit -> result in x_out                             */
+    double queue_ms;       /* submit -> admitted to the GPU                         */
+    uint64_t factor_id;    /* resident factor (0 if none)                           */
+} bss_request_info;
+
+typedef struct {
+    int64_t submitted, completed, failed, evictions;
+    int64_t resident_factors;
+    int64_t bytes_in_use, bytes_peak;
+    double p50_ms, p99_ms, mean_ms, max_ms;  /* latency over completed requests  */
+    double busy_s;                            /* first submit -> last completion  */
+} bss_server_stats;
+
+void bss_server_default_options(bss_server_options *opt);
+int bss_server_create(const bss_server_options *opt, bss_server **out);
+/* Waits for every request, frees all device memory and stops the worker. */
+int bss_server_destroy(bss_server *s);
+/* A new system (A, B, d host arrays). keep != 0: its factor stays resident;
+ * *factor_id names it (also returned in the info). */
+int bss_server_submit(bss_server *s, int64_t N, int64_t n, int64_t k, const double *A, const double *B,
+                      const double *d, int32_t keep, double *x_out, uint64_t *request_id, uint64_t *factor_id);
+/* A new Kalman-smoother system from its model and observations (host
+ * arrays, meaning as in bss_kf_build); blocks are built on the device. */
+int bss_server_submit_kalman(bss_server *s, int64_t N, int64_t n, int64_t m, int64_t k, const double *F,
+                             const double *H, const double *Qinv, const double *Rinv, const double *P0inv,
+                             const double *x0, const double *y, int32_t keep, double *x_out, uint64_t *request_id,
+                             uint64_t *factor_id);
+/* A repeat right-hand side on a resident factor: d (n x k x N) for a
+ * system factor, or y (m x k x N) for a Kalman factor (d rebuilt on the
+ * device).  Runs after the factor's earlier requests. */
+int bss_server_submit_rhs(bss_server *s, uint64_t factor_id, const double *d_or_y, double *x_out,
+                          uint64_t *request_id);
+/* Blocks until the request finished; fills *info (may be NULL); returns its
+ * status.  A request id can be waited on once. */
+int bss_server_wait(bss_server *s, uint64_t request_id, bss_request_info *info);
+/* *done = 1 when the request finished (does not consume it). */
+int bss_server_poll(bss_server *s, uint64_t request_id, int32_t *done);
+/* Drops a resident factor (after its pending requests). */
+int bss_server_release(bss_server *s, uint64_t factor_id);
+int bss_server_get_stats(bss_server *s, bss_server_stats *stats);
+/* Clears the latency record and counters (not the resident factors). */
+int bss_server_reset_stats(bss_server *s);
+
 /* Number of CUDA kernels this library has launched in this process, over
  * all handles (no counterpart in the reference; benchmarks report it). */
 int64_t bss_kernel_launches(void);

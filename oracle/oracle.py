@@ -228,29 +228,67 @@ def gen_config2(rng: np.random.Generator, N: int, n: int, k: int = 4,
     return A, B, d
 
 
-def gen_kalman(rng: np.random.Generator, N: int, n: int, k: int = 1):
-    """BASELINE config 4 (Kalman-smoother normal equations), uniform blocks:
+def gen_kalman_model(rng: np.random.Generator, N: int, n: int, k: int = 1):
+    """BASELINE config 4 model (Kalman-smoother normal equations):
     F ~ N(0,1) rescaled to spectral radius 0.95, H ~ N(0,1) (n/2 x n),
-    Q = 0.1 I, R = 0.5 I; A_i = Q^-1 + F^T Q^-1 F + H^T R^-1 H,
-    B_i = -F^T Q^-1; d_i = H^T R^-1 y_i from a simulated trajectory
-    (benchmark/benchmark_kf.jl:79-102,147-150 form)."""
+    Q = 0.1 I, R = 0.5 I, k observation sequences Y (N, m, k) simulated from
+    the model (benchmark/benchmark_kf.jl:79-102 form).  Returns
+    (F, H, Qinv, Rinv, Y)."""
     m = max(n // 2, 1)
     F = rng.standard_normal((n, n))
     F *= 0.95 / max(np.max(np.abs(np.linalg.eigvals(F))), 1e-30)
     H = rng.standard_normal((m, n))
-    qinv = 1.0 / 0.1
-    rinv = 1.0 / 0.5
-    Ablk = qinv * np.eye(n) + qinv * (F.T @ F) + rinv * (H.T @ H)
-    Bblk = -qinv * F.T
-    A = np.broadcast_to(Ablk, (N, n, n)).copy()
-    B = np.broadcast_to(Bblk, (max(N - 1, 0), n, n)).copy()
-    d = np.empty((N, n, k))
+    Y = np.empty((N, m, k))
     for j in range(k):
         xs = np.zeros(n)
         for i in range(N):
             xs = F @ xs + math.sqrt(0.1) * rng.standard_normal(n)
-            y = H @ xs + math.sqrt(0.5) * rng.standard_normal(m)
-            d[i, :, j] = rinv * (H.T @ y)
+            Y[i, :, j] = H @ xs + math.sqrt(0.5) * rng.standard_normal(m)
+    return F, H, np.eye(n) / 0.1, np.eye(m) / 0.5, Y
+
+
+def gen_kalman(rng: np.random.Generator, N: int, n: int, k: int = 1):
+    """BASELINE config 4 blocks, uniform: A_i = Q^-1 + F^T Q^-1 F + H^T R^-1 H,
+    B_i = -F^T Q^-1, d_i = H^T R^-1 y_i (benchmark/benchmark_kf.jl:79-102,
+    147-150 form) from gen_kalman_model."""
+    F, H, Qinv, Rinv, Y = gen_kalman_model(rng, N, n, k)
+    return kf_blocks(F, H, Qinv, Rinv, Y)
+
+
+def kf_blocks(F, H, Qinv, Rinv, Y, P0inv=None, x0=None):
+    """Normal equations of the Kalman smoother, restating build_kf_blocks
+    (benchmark/benchmark_kf.jl:105-154) with the inverses given:
+    F (n,n), H (m,n), Qinv (n,n), Rinv (m,m), Y (N,m,k) -> A (N,n,n),
+    B (N-1,n,n), d (N,n,k).  With P0inv: A_1 += P0inv (no Q^-1), A_N has no
+    F^T Q^-1 F (the reference's boundary blocks); without it every A_i is
+    H^T R^-1 H + Q^-1 + F^T Q^-1 F.  A_i is taken from its upper triangle
+    (Symmetric(Akk))."""
+    N = Y.shape[0]
+    n = F.shape[0]
+    QF = Qinv @ F
+    FQF = F.T @ QF
+    HRH = H.T @ (Rinv @ H)
+    Bup = -QF.T
+
+    def sym_upper(M):
+        U = np.triu(M)
+        return U + np.triu(M, 1).T
+
+    Aint = sym_upper(HRH + Qinv + FQF)
+    if P0inv is not None:
+        Afirst = sym_upper(HRH + P0inv + FQF)
+        Alast = sym_upper(HRH + Qinv)
+    else:
+        Afirst = Alast = Aint
+    A = np.broadcast_to(Aint, (N, n, n)).copy()
+    A[0] = Afirst
+    if N > 1:
+        A[N - 1] = Alast
+    B = np.broadcast_to(Bup, (max(N - 1, 0), n, n)).copy()
+    RH = Rinv @ H
+    d = np.einsum("mn,imk->ink", RH, Y)
+    if P0inv is not None and x0 is not None:
+        d[0] += (P0inv @ x0)[:, None]
     return A, B, d
 
 
