@@ -43,6 +43,11 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="skip the secondary legs")
+    ap.add_argument("--no-extra", action="store_true", help="skip the config 2/3 and served legs")
+    ap.add_argument("--case", default=None,
+                    help="run one small named case for a profiler and exit: "
+                         "chain_n64 (N=4096, n=64, mixed), wide_n128 (N=2048, n=128, mixed), "
+                         "batch_small (64 uneven systems, mixed)")
     return ap.parse_args()
 
 
@@ -364,6 +369,14 @@ def run_ours(args):
         except Exception as e:  # pragma: no cover
             cpu_base = {"value": None, "unit": "solves/s", "cores": None, "kind": "port", "sample": f"failed: {e}"}
 
+    others = {}
+    if not args.quick and not args.no_extra:
+        del A, B, d
+        torch.cuda.empty_cache()
+        others["config2_single_system"] = run_config2(bss, dev)
+        others["uneven_batch"] = run_config3(bss, dev)
+        others["served_kalman"] = run_served_legs(bss)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
@@ -381,6 +394,7 @@ def run_ours(args):
             "clocks": clocks, "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e,
         }
         line.update(extra)
+        line.update(others)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.barrier()
@@ -519,6 +533,169 @@ def run_served(bss, precision, models, reqs, budget=100 * 10**9, streams=8):
             "mean_refine_steps": (sum(steps) / len(steps)) if steps else None}
 
 
+# --------------------------------------------------------------------------
+# config 2 (one large system, wide blocks) and config 3 (uneven batch)
+# --------------------------------------------------------------------------
+def _orthogonal(G):
+    """Q of the QR factorization of G (positive diagonal R) by CholeskyQR2:
+    Q1 = G R1^{-1} with R1 = chol(G^T G), then the same once more on Q1."""
+    import torch
+    Q = G
+    for _ in range(2):
+        R = torch.linalg.cholesky(Q.transpose(1, 2) @ Q, upper=True)
+        Q = torch.linalg.solve_triangular(R, Q, upper=True, left=False)
+    return Q
+
+
+def gen_config2(dev, N=65536, n=128, k=4, seed=2):
+    """A_i = Q_i diag(lambda) Q_i^T (lambda log-spaced over [1, 1e4]),
+    B_i = 0.45 U_i V_i^T, d ~ N(0,1); Q, U, V orthogonal factors of
+    Gaussian matrices.  Column-major (n, n, N) views."""
+    import torch
+    g = torch.Generator(device=dev).manual_seed(seed)
+    lam = torch.logspace(0, 4, n, dtype=torch.float64, device=dev)
+    A = torch.empty((N, n, n), dtype=torch.float64, device=dev)
+    B = torch.empty((N - 1, n, n), dtype=torch.float64, device=dev)
+    ch = 8192
+    for s0 in range(0, N, ch):
+        e = min(N, s0 + ch)
+        Q = _orthogonal(torch.randn((e - s0, n, n), dtype=torch.float64, device=dev, generator=g))
+        Ab = (Q * lam[None, None, :]) @ Q.transpose(1, 2)
+        A[s0:e] = 0.5 * (Ab + Ab.transpose(1, 2))
+    for s0 in range(0, N - 1, ch):
+        e = min(N - 1, s0 + ch)
+        U = _orthogonal(torch.randn((e - s0, n, n), dtype=torch.float64, device=dev, generator=g))
+        V = _orthogonal(torch.randn((e - s0, n, n), dtype=torch.float64, device=dev, generator=g))
+        B[s0:e] = 0.45 * (U @ V.transpose(1, 2))
+    d = torch.randn((N, n, k), dtype=torch.float64, device=dev, generator=g)
+    return A.permute(1, 2, 0), B.permute(1, 2, 0), d.permute(1, 2, 0)
+
+
+def _timed_handle_leg(bss, A, B, d, precision, reps):
+    """factorize!+solve! of one system on the device, inputs copied into the
+    handle before each rep (outside the timed region); median ms."""
+    import torch
+    n, _, N = A.shape
+    k = d.shape[1]
+    data = bss.initialize_batched(N, n, torch.float64, k=k, precision=precision)
+    At, Bt, dt = data.A_tensor[:, :, :N], data.B_tensor[:, :, :N - 1], data.d_tensor[:, :, :N]
+    fac, sol = [], []
+    for r in range(reps + 1):
+        At.copy_(A)
+        Bt.copy_(B)
+        dt.copy_(d)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record()
+        bss.factorize_(data)
+        e1.record()
+        bss.solve_(data)
+        e2.record()
+        bss.synchronize(data)
+        torch.cuda.synchronize()
+        if r > 0 or reps == 0:
+            fac.append(e0.elapsed_time(e1))
+            sol.append(e1.elapsed_time(e2))
+    info = bss.get_info(data)
+    relres = rel_residual_dev(A, B, dt, d)
+    del data
+    torch.cuda.empty_cache()
+    f, s_ = statistics.median(fac), statistics.median(sol)
+    return {"solves_per_s": 1e3 / (f + s_), "factor_ms": f, "solve_ms": s_, "rel_residual": relres,
+            "refine_steps": info["refine_steps"], "levels": info["levels"]}
+
+
+def run_config2(bss, dev):
+    import torch
+    A, B, d = gen_config2(dev)
+    out = {"workload": "N=65536, n=128, k=4, A_i=Q diag(logspace(0,4)) Q^T, B_i=0.45 U V^T, d~N(0,1)",
+           "mixed": _timed_handle_leg(bss, A, B, d, "mixed", 3),
+           "plain_fp64": _timed_handle_leg(bss, A, B, d, "plain", 1)}
+    out["mixed_over_plain_fp64"] = out["mixed"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
+    del A, B, d
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_config3(bss, dev, steps=3, seed=3):
+    """2048 independent systems, N ~ U{16..1024}, n from {16,32,48,64,96,128},
+    k ~ U{1..8}, A_i = G G^T + 2n I, B_i ~ 0.5 N(0,1), d ~ U[0,1); mixed
+    precision, one batch (graph-replayed after the first call)."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(seed)
+    S = 2048
+    Ns = rng.integers(16, 1025, S)
+    ns = rng.choice([16, 32, 48, 64, 96, 128], S)
+    ks = rng.integers(1, 9, S)
+    res = {"workload": "2048 systems, N~U{16..1024}, n in {16,32,48,64,96,128}, k~U{1..8}, "
+                       "A=GG^T+2nI, B~0.5N(0,1)"}
+    def fill(b):  # seeded inputs written straight into the batch tensors
+        g = torch.Generator(device=dev).manual_seed(seed)
+        for sv in b.systems:
+            N, n, k = sv.N, sv.n, sv.k
+            G = torch.randn((N, n, n), dtype=torch.float64, device=dev, generator=g)
+            sv.A_tensor.copy_((G @ G.transpose(1, 2) + 2 * n * torch.eye(n, dtype=torch.float64, device=dev))
+                              .permute(1, 2, 0))
+            Bm = 0.5 * torch.randn((max(N - 1, 0), n, n), dtype=torch.float64, device=dev, generator=g)
+            if N > 1:
+                sv.B_tensor.copy_(Bm.permute(1, 2, 0))
+            sv.d_tensor.copy_(torch.rand((N, n, k), dtype=torch.float64, device=dev, generator=g).permute(1, 2, 0))
+
+    def leg(prec):  # in its own scope: the batch dies with the function's locals
+        b = bss.initialize_multi(Ns.tolist(), ns.tolist(), ks.tolist(), torch.float64, precision=prec)
+        fac, sol = [], []
+        nsteps = steps if prec == "mixed" else 1
+        dsave = None
+        for r in range(nsteps + 1):
+            if prec == "plain" or dsave is None:  # plain factors in place: fresh inputs every rep
+                fill(b)
+                if prec == "mixed":
+                    dsave = [sv.d_tensor.clone() for sv in b.systems]
+            else:
+                for sv, dm in zip(b.systems, dsave):
+                    sv.d_tensor.copy_(dm)
+            torch.cuda.synchronize()
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record()
+            b.factorize()
+            e1.record()
+            b.solve()
+            e2.record()
+            b.synchronize()
+            torch.cuda.synchronize()
+            if r > 0:
+                fac.append(e0.elapsed_time(e1))
+                sol.append(e1.elapsed_time(e2))
+        f, s_ = statistics.median(fac), statistics.median(sol)
+        out = {"systems_per_s": S * 1e3 / (f + s_), "factor_ms": f, "solve_ms": s_}
+        if prec == "mixed":
+            out["worst_rel_residual"] = max(b.info(i)["rel_residual"] for i in range(S))
+            out["max_refine_steps"] = max(b.info(i)["refine_steps"] for i in range(S))
+        return out
+
+    import gc
+    for prec in ("mixed", "plain"):
+        res["mixed" if prec == "mixed" else "plain_fp64"] = leg(prec)
+        gc.collect()
+        torch.cuda.empty_cache()
+    res["mixed_over_plain_fp64"] = res["mixed"]["systems_per_s"] / res["plain_fp64"]["systems_per_s"]
+    return res
+
+
+def run_served_legs(bss, n_requests=1200, rate=2000.0):
+    models, reqs = gen_kf_stream(n_requests, rate)
+    out = {"workload": f"{n_requests} Kalman-smoother requests, n in {{8,16,32,64}}, N~U{{50..5000}}, "
+                       f"Poisson {rate:g} req/s, 30% repeat RHS on resident factors, 100 GB budget"}
+    out["mixed"] = run_served(bss, "mixed", models, reqs)
+    out["plain_fp64"] = run_served(bss, "plain", models, reqs)
+    sat = [dict(r, t=0.0) for r in reqs]
+    out["saturated_mixed"] = run_served(bss, "mixed", models, sat)
+    out["saturated_plain_fp64"] = run_served(bss, "plain", models, sat)
+    out["saturated_mixed_over_plain_fp64"] = (out["saturated_mixed"]["solves_per_s"] /
+                                              out["saturated_plain_fp64"]["solves_per_s"])
+    return out
+
+
 def roofline_chain_factor(bss, A, B, d, hbm_gbs, peak_kind):
     """Roofline of the dominant kernel of the mixed path: the level-0 chain
     factor kernel (FP64 A_i, B_i in; FP32 V_i, W_i, Y_i out).  Algorithmic
@@ -559,8 +736,56 @@ def roofline_chain_factor(bss, A, B, d, hbm_gbs, peak_kind):
             "note": "latency/FMA-bound chain: the HBM fraction is low by construction"}
 
 
+def run_case(name, reps=3):
+    """A small workload for profiler captures: `reps` factorize!+solve! calls."""
+    import numpy as np
+    import torch
+    import blockstructuredsolvers_gb300 as bss
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev).manual_seed(5)
+    if name in ("chain_n64", "wide_n128"):
+        N, n = (4096, 64) if name == "chain_n64" else (2048, 128)
+        G = torch.randn((N, n, n), dtype=torch.float64, device=dev, generator=g)
+        A = (G @ G.transpose(1, 2) + n * torch.eye(n, dtype=torch.float64, device=dev)).permute(1, 2, 0)
+        B = torch.randn((N - 1, n, n), dtype=torch.float64, device=dev, generator=g).permute(1, 2, 0)
+        d = torch.rand((N, n, 1), dtype=torch.float64, device=dev, generator=g).permute(1, 2, 0)
+        data = bss.initialize_batched(N, n, torch.float64, precision="mixed")
+        data.A_tensor[:, :, :N].copy_(A)
+        data.B_tensor[:, :, :N - 1].copy_(B)
+        for _ in range(reps):
+            data.d_tensor[:, :, :N].copy_(d)
+            bss.factorize_(data)
+            bss.solve_(data)
+        bss.synchronize(data)
+    elif name == "batch_small":
+        rng = np.random.default_rng(1)
+        S = 64
+        Ns, ns, ks = rng.integers(16, 1025, S), rng.choice([16, 32, 48, 64, 96, 128], S), rng.integers(1, 9, S)
+        b = bss.initialize_multi(Ns.tolist(), ns.tolist(), ks.tolist(), torch.float64, precision="mixed")
+        for sv in b.systems:
+            N, n, k = sv.N, sv.n, sv.k
+            G = torch.randn((N, n, n), dtype=torch.float64, device=dev, generator=g)
+            sv.A_tensor.copy_((G @ G.transpose(1, 2) + 2 * n * torch.eye(n, dtype=torch.float64, device=dev))
+                              .permute(1, 2, 0))
+            if N > 1:
+                sv.B_tensor.copy_(0.5 * torch.randn((N - 1, n, n), dtype=torch.float64, device=dev,
+                                                    generator=g).permute(1, 2, 0))
+            sv.d_tensor.copy_(torch.rand((N, n, k), dtype=torch.float64, device=dev, generator=g).permute(1, 2, 0))
+        for _ in range(reps):
+            b.factorize()
+            b.solve()
+        b.synchronize()
+    else:
+        raise SystemExit(f"unknown case {name}")
+    torch.cuda.synchronize()
+    print(json.dumps({"case": name, "reps": reps, "ok": True}))
+
+
 def main():
     args = parse()
+    if args.case:
+        run_case(args.case)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
