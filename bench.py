@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--case", default=None,
                     help="run one small named case for a profiler and exit: "
                          "chain_n64 (N=4096, n=64, mixed), wide_n128 (N=2048, n=128, mixed), "
-                         "batch_small (64 uneven systems, mixed)")
+                         "batch_small (64 uneven systems, mixed), batch_2048 (the 2048-system batch, mixed)")
     return ap.parse_args()
 
 
@@ -757,9 +757,9 @@ def run_case(name, reps=3):
             bss.factorize_(data)
             bss.solve_(data)
         bss.synchronize(data)
-    elif name == "batch_small":
-        rng = np.random.default_rng(1)
-        S = 64
+    elif name in ("batch_small", "batch_2048"):
+        rng = np.random.default_rng(1 if name == "batch_small" else 3)
+        S = 64 if name == "batch_small" else 2048
         Ns, ns, ks = rng.integers(16, 1025, S), rng.choice([16, 32, 48, 64, 96, 128], S), rng.integers(1, 9, S)
         b = bss.initialize_multi(Ns.tolist(), ns.tolist(), ks.tolist(), torch.float64, precision="mixed")
         for sv in b.systems:

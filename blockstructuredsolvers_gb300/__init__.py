@@ -26,7 +26,8 @@ from ._lib import BSSError, NotSPDError  # noqa: F401
 __all__ = [
     "BlockTriDiagData_batched", "BlockTriDiagData_seq", "initialize_batched", "initialize_seq",
     "factorize_", "solve_", "factorize", "solve", "synchronize", "get_info", "residual",
-    "plan_reference", "BSSError", "NotSPDError", "MultiSystemBatch", "initialize_multi", "Server", "kf_build",
+    "plan_reference", "BSSError", "NotSPDError", "MultiSystemBatch", "initialize_multi", "Server", "kf_build", "BlockTriDiagData_cpu", "initialize_cpu",
+    "autotune", "autotune_lookup", "autotune_save", "autotune_load", "autotune_clear",
 ]
 
 
@@ -174,18 +175,86 @@ def initialize_seq(N: int, n: int, T=None, M=None, *, k: int = 1, stream=None) -
     return BlockTriDiagData_seq(_Handle(h.value), tdt, int(N))
 
 
-def factorize_(data: _Data, check: bool = False) -> None:
-    """factorize!(data) (src/gpu_batched.jl:184-227 / src/gpu_seq.jl:61-71).
-    Asynchronous on the handle's stream; ``check=True`` waits and raises
-    NotSPDError if a pivot failed."""
+class _CpuHandle:
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                _lib.load().bss_cpu_destroy(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+
+class BlockTriDiagData_cpu:
+    """``BlockTriDiagData_cpu`` (src/cpu.jl:1-10): N, n and A_list, B_list,
+    d_list -- numpy views of the handle's host memory (column-major blocks,
+    also exposed whole as A_tensor (n,n,N), B_tensor, d_tensor)."""
+
+    def __init__(self, handle: _CpuHandle, N, n, k, np_dtype):
+        import numpy as np
+        self._h = handle
+        self.N, self.n, self.k = N, n, k
+        A = ctypes.c_void_p()
+        B = ctypes.c_void_p()
+        d = ctypes.c_void_p()
+        _lib.check(_lib.load().bss_cpu_get_tensors(handle.ptr, ctypes.byref(A), ctypes.byref(B), ctypes.byref(d)))
+        es = np.dtype(np_dtype).itemsize
+        ct = ctypes.c_double if es == 8 else ctypes.c_float
+
+        def view(ptr, r, c, cnt):
+            buf = (ct * (r * c * max(cnt, 1))).from_address(ptr)
+            return np.ndarray((r, c, cnt), dtype=np_dtype, buffer=buf, strides=(es, es * r, es * r * c))
+
+        self.A_tensor = view(A.value, n, n, N)
+        self.B_tensor = view(B.value, n, n, N - 1)
+        self.d_tensor = view(d.value, n, k, N)
+        self.A_list = [self.A_tensor[:, :, i] for i in range(N)]
+        self.B_list = [self.B_tensor[:, :, i] for i in range(N - 1)]
+        self.d_list = [self.d_tensor[:, :, i] for i in range(N)]
+
+    @property
+    def handle(self):
+        return self._h.ptr
+
+
+def initialize_cpu(N: int, n: int, T=None, *, k: int = 1) -> BlockTriDiagData_cpu:
+    """initialize_cpu(N, n, T) (src/cpu.jl:12-29): zeroed host blocks."""
+    import numpy as np
+    if T in (None, float, "float64", "Float64", "f64", np.float64):
+        code, npt = _lib.BSS_F64, np.float64
+    elif T in ("float32", "Float32", "f32", np.float32):
+        code, npt = _lib.BSS_F32, np.float32
+    else:
+        torch = _torch()
+        code = _dtype_code(T)[0]
+        npt = np.float64 if code == _lib.BSS_F64 else np.float32
+    h = ctypes.c_void_p()
+    _lib.check(_lib.load().bss_cpu_create(int(N), int(n), int(k), code, ctypes.byref(h)))
+    return BlockTriDiagData_cpu(_CpuHandle(h.value), int(N), int(n), int(k), npt)
+
+
+def factorize_(data, check: bool = False) -> None:
+    """factorize!(data) (src/gpu_batched.jl:184-227 / src/gpu_seq.jl:61-71 /
+    src/cpu.jl:31-40).  GPU handles: asynchronous on the handle's stream;
+    ``check=True`` waits and raises NotSPDError if a pivot failed.  CPU
+    data: synchronous, raises NotSPDError on a failed pivot."""
+    if isinstance(data, BlockTriDiagData_cpu):
+        _lib.check(_lib.load().bss_cpu_factorize(data.handle))
+        return
     _lib.check(_lib.load().bss_factorize(data.handle))
     if check:
         synchronize(data)
 
 
-def solve_(data: _Data, check: bool = False) -> None:
-    """solve!(data) (src/gpu_batched.jl:229-258 / src/gpu_seq.jl:73-84):
-    d_tensor <- A^{-1} d_tensor."""
+def solve_(data, check: bool = False) -> None:
+    """solve!(data) (src/gpu_batched.jl:229-258 / src/gpu_seq.jl:73-84 /
+    src/cpu.jl:42-50): d_tensor <- A^{-1} d_tensor."""
+    if isinstance(data, BlockTriDiagData_cpu):
+        _lib.check(_lib.load().bss_cpu_solve(data.handle))
+        return
     _lib.check(_lib.load().bss_solve(data.handle))
     if check:
         synchronize(data)
@@ -339,6 +408,41 @@ def initialize_multi(Ns, ns, ks=None, T=None, *, precision: str = "plain", max_r
 
 def plan_reference(N: int):
     return _lib.plan_reference(N)
+
+
+def _tune_key(n, T, precision):
+    code, _ = _dtype_code(_torch().float64 if T is None else T)
+    prec = {"plain": _lib.BSS_PRECISION_PLAIN, "mixed": _lib.BSS_PRECISION_MIXED}[precision]
+    return int(n), code, prec
+
+
+def autotune(n, T=None, precision="mixed", N_probe=16384) -> dict:
+    """Time candidate plans for block size n and keep the fastest (see
+    bss_autotune in include/bss.h); later handles, batches and server
+    requests with default options use it."""
+    e = _lib.TuneEntry()
+    n, code, prec = _tune_key(n, T, precision)
+    _lib.check(_lib.load().bss_autotune(n, code, prec, int(N_probe), ctypes.byref(e)))
+    return {k: getattr(e, k) for k, _ in _lib.TuneEntry._fields_}
+
+
+def autotune_lookup(n, T=None, precision="mixed"):
+    e = _lib.TuneEntry()
+    n, code, prec = _tune_key(n, T, precision)
+    rc = _lib.load().bss_autotune_lookup(n, code, prec, ctypes.byref(e))
+    return None if rc else {k: getattr(e, k) for k, _ in _lib.TuneEntry._fields_}
+
+
+def autotune_save(path):
+    _lib.check(_lib.load().bss_autotune_save(str(path).encode()))
+
+
+def autotune_load(path):
+    _lib.check(_lib.load().bss_autotune_load(str(path).encode()))
+
+
+def autotune_clear():
+    _lib.load().bss_autotune_clear()
 
 
 def _ptr(a):

@@ -41,6 +41,9 @@ EXPORTS = (
     "bss_kf_build", "bss_server_default_options", "bss_server_create", "bss_server_destroy", "bss_server_submit",
     "bss_server_submit_kalman", "bss_server_submit_rhs", "bss_server_wait", "bss_server_poll",
     "bss_server_release", "bss_server_get_stats", "bss_server_reset_stats",
+    "bss_autotune", "bss_autotune_lookup", "bss_autotune_clear", "bss_autotune_save", "bss_autotune_load",
+    "bss_cpu_create", "bss_cpu_destroy", "bss_cpu_get_tensors", "bss_cpu_factorize", "bss_cpu_solve",
+    "bss_cpu_failed_block",
 )
 
 
@@ -93,6 +96,19 @@ class ServerStats(ctypes.Structure):
         ("mean_ms", ctypes.c_double),
         ("max_ms", ctypes.c_double),
         ("busy_s", ctypes.c_double),
+    ]
+
+
+class TuneEntry(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int32),
+        ("dtype", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("wave_mult_x4", ctypes.c_int32),
+        ("seq_cutoff", ctypes.c_int32),
+        ("chain_blocks", ctypes.c_int32),
+        ("single_ms", ctypes.c_double),
+        ("batch_ms", ctypes.c_double),
     ]
 
 
@@ -180,9 +196,21 @@ def load(path: str | None = None):
     L.bss_server_release.argtypes = [vp, u64]
     L.bss_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
     L.bss_server_reset_stats.argtypes = [vp]
+    L.bss_autotune.argtypes = [i64, i32, i32, i64, ctypes.POINTER(TuneEntry)]
+    L.bss_autotune_lookup.argtypes = [i64, i32, i32, ctypes.POINTER(TuneEntry)]
+    L.bss_autotune_clear.argtypes = []
+    L.bss_autotune_clear.restype = None
+    L.bss_autotune_save.argtypes = [ctypes.c_char_p]
+    L.bss_autotune_load.argtypes = [ctypes.c_char_p]
+    L.bss_cpu_create.argtypes = [i64, i64, i64, i32, ctypes.POINTER(vp)]
+    L.bss_cpu_destroy.argtypes = [vp]
+    L.bss_cpu_get_tensors.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    L.bss_cpu_factorize.argtypes = [vp]
+    L.bss_cpu_solve.argtypes = [vp]
+    L.bss_cpu_failed_block.argtypes = [vp, ctypes.POINTER(i64)]
     for name in EXPORTS:
         if name not in ("bss_default_options", "bss_last_error_string", "bss_version", "bss_kernel_launches",
-                        "bss_server_default_options"):
+                        "bss_server_default_options", "bss_autotune_clear"):
             getattr(L, name).restype = ctypes.c_int
     if path is None:
         _lib = L

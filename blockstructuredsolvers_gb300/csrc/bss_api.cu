@@ -203,12 +203,16 @@ int bss::plan_handle(bss_handle *h)
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
             const int t0 = mixed ? F32 : D;
             const int tin0 = D;
+            bss_tune_entry te{};
+            const bool tuned = tuned_plan((int)n, D, h->opt.precision, &te);
+            const long long wave = (long long)sms * chain_ctas_per_sm(tin0, t0, (int)n);
             long long target = h->opt.target_partitions > 0
                                    ? h->opt.target_partitions
-                                   : (long long)sms * chain_ctas_per_sm(tin0, t0, (int)n);
+                                   : (tuned ? std::max(1LL, wave * te.wave_mult_x4 / 4) : wave);
             // mixed: the coarsest level is FP64, whose per-SM rate is ~1/64 of FP32,
             // so halve down to 2 blocks; plain: 4 balances levels against chain length
-            long long cutoff = h->opt.seq_cutoff > 0 ? h->opt.seq_cutoff : (mixed ? 2 : 4);
+            long long cutoff = h->opt.seq_cutoff > 0 ? h->opt.seq_cutoff
+                                                     : (tuned ? te.seq_cutoff : (mixed ? 2 : 4));
             plan_auto(h->N, target, cutoff, Ns, Qs, coarsest);
         }
     }

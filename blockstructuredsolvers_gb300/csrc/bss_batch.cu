@@ -111,10 +111,14 @@ size_t put_vec(Blob &b, const std::vector<T> &v)
 
 int nb_class(long long n) { return tile_for((int)n); }
 
-// finest-level blocks per partition of every batch system
-long long batch_chain_blocks(const bss_options &o, int /*n*/)
+// finest-level blocks per partition of every batch system: the caller's
+// value, else the autotuner's for (n, dtype, precision), else 32 (mixed) /
+// 128 (plain)
+long long batch_chain_blocks(const bss_options &o, int n, int dtype)
 {
     if (o.chain_blocks > 0) return o.chain_blocks;
+    bss_tune_entry te{};
+    if (tuned_plan(n, dtype, o.precision, &te) && te.chain_blocks > 0) return te.chain_blocks;
     return o.precision == BSS_PRECISION_MIXED ? 32 : 128;
 }
 
@@ -293,7 +297,7 @@ void plan_asm_schur(Builder &B, int level)
 
 // forward sweeps (and the coarsest level's full solve) of one level
 template <class T>
-void plan_fwd(Builder &B, int level, bool coarsest, bool staged, std::vector<std::function<Step(char *)>> &dst)
+void plan_fwd(Builder &B, int level, bool coarsest, bool staged, int nb, std::vector<std::function<Step(char *)>> &dst)
 {
     bss_batch *b = B.b;
     std::vector<SolveArgs<T>> descs;
@@ -307,7 +311,7 @@ void plan_fwd(Builder &B, int level, bool coarsest, bool staged, std::vector<std
         if (l >= L) continue;
         const Level &lv = h->levels[l];
         if (lv.seq != coarsest || (lv.t == F64) != std::is_same<T, double>::value) continue;
-        if (solve_staged<T>((int)h->n, (int)h->k) != staged) continue;
+        if (solve_staged<T>((int)h->n, (int)h->k) != staged || nb_class(h->n) != nb) continue;
         const int di = (int)descs.size();
         descs.push_back(make_solve_args<T>(h, l, 0, (int)h->k));
         smem = std::max(smem, solve_smem_bytes<T>((int)h->n, (int)h->k, staged));
@@ -373,7 +377,7 @@ void plan_asm_rhs(Builder &B, int level, std::vector<std::function<Step(char *)>
 }
 
 template <class T, class Tsep>
-void plan_bwd(Builder &B, int level, bool staged, std::vector<std::function<Step(char *)>> &dst)
+void plan_bwd(Builder &B, int level, bool staged, int nb, std::vector<std::function<Step(char *)>> &dst)
 {
     bss_batch *b = B.b;
     std::vector<SolveArgs<T>> descs;
@@ -386,7 +390,7 @@ void plan_bwd(Builder &B, int level, bool staged, std::vector<std::function<Step
         const Level &L = h->levels[level], &X = h->levels[level + 1];
         if ((L.t == F64) != std::is_same<T, double>::value || (X.t == F64) != std::is_same<Tsep, double>::value)
             continue;
-        if (solve_staged<T>((int)h->n, (int)h->k) != staged) continue;
+        if (solve_staged<T>((int)h->n, (int)h->k) != staged || nb_class(h->n) != nb) continue;
         const int di = (int)descs.size();
         descs.push_back(make_solve_args<T>(h, level, 0, (int)h->k));
         smem = std::max(smem, solve_smem_bytes<T>((int)h->n, (int)h->k, staged));
@@ -418,25 +422,32 @@ void plan_bwd(Builder &B, int level, bool staged, std::vector<std::function<Step
 // one full chain solve of every system on its level-0 RHS (levels[0].d)
 void plan_chain_solve(Builder &B, int maxpart, std::vector<std::function<Step(char *)>> &dst)
 {
+    // one launch per (type, staged form, block-size class): the shared
+    // memory of a launch is sized for its largest system, so mixing classes
+    // would cap every CTA at the occupancy of the largest blocks
+    static const int kClasses[] = {16, 32, 64, WIDE_CLASS};
     for (int l = 0; l < maxpart; ++l) {
-        for (bool st : {true, false}) {
-            plan_fwd<float>(B, l, false, st, dst);
-            plan_fwd<double>(B, l, false, st, dst);
-        }
+        for (bool st : {true, false})
+            for (int nb : kClasses) {
+                plan_fwd<float>(B, l, false, st, nb, dst);
+                plan_fwd<double>(B, l, false, st, nb, dst);
+            }
         plan_asm_rhs<float, float>(B, l, dst);
         plan_asm_rhs<float, double>(B, l, dst);
         plan_asm_rhs<double, double>(B, l, dst);
     }
-    for (bool st : {true, false}) {
-        plan_fwd<float>(B, 0, true, st, dst);
-        plan_fwd<double>(B, 0, true, st, dst);
-    }
-    for (int l = maxpart - 1; l >= 0; --l)
-        for (bool st : {true, false}) {
-            plan_bwd<float, float>(B, l, st, dst);
-            plan_bwd<float, double>(B, l, st, dst);
-            plan_bwd<double, double>(B, l, st, dst);
+    for (bool st : {true, false})
+        for (int nb : kClasses) {
+            plan_fwd<float>(B, 0, true, st, nb, dst);
+            plan_fwd<double>(B, 0, true, st, nb, dst);
         }
+    for (int l = maxpart - 1; l >= 0; --l)
+        for (bool st : {true, false})
+            for (int nb : kClasses) {
+                plan_bwd<float, float>(B, l, st, nb, dst);
+                plan_bwd<float, double>(B, l, st, nb, dst);
+                plan_bwd<double, double>(B, l, st, nb, dst);
+            }
 }
 
 template <class Tc>
@@ -470,7 +481,7 @@ void plan_vec(Builder &B, int op, std::vector<std::function<Step(char *)>> &dst)
 }
 
 template <class Tr>
-void plan_resid(Builder &B, std::vector<std::function<Step(char *)>> &dst)
+void plan_resid(Builder &B, int nb, std::vector<std::function<Step(char *)>> &dst)
 {
     bss_batch *b = B.b;
     std::vector<ResidualDesc<Tr>> descs;
@@ -478,8 +489,8 @@ void plan_resid(Builder &B, std::vector<std::function<Step(char *)>> &dst)
     size_t smem = 0;
     for (int s = 0; s < b->nsys; ++s) {
         bss_handle *h = b->sys[s];
-        if ((h->levels[0].t == F64) != std::is_same<Tr, double>::value) continue;
-        const long long per = std::max(1LL, std::min(h->N, 64LL));
+        if ((h->levels[0].t == F64) != std::is_same<Tr, double>::value || nb_class(h->n) != nb) continue;
+        const long long per = std::max(1LL, std::min(h->N, 32LL));
         int kc = (int)h->k;  // column chunk whose shared memory fits
         while (kc > 1 && residual_smem_bytes<double>((int)h->n, kc) > (size_t)200 * 1024) kc = (kc + 1) / 2;
         for (int j0 = 0; j0 < h->k; j0 += kc) {
@@ -548,8 +559,10 @@ int build_batch(bss_batch *b)
         plan_chain_solve(B, maxpart, B.pro);
         plan_vec<float>(B, VEC_SET, B.pro);
         plan_vec<double>(B, VEC_SET, B.pro);
-        plan_resid<float>(B, B.resid);
-        plan_resid<double>(B, B.resid);
+        for (int nb : {16, 32, 64, (int)WIDE_CLASS}) {
+            plan_resid<float>(B, nb, B.resid);
+            plan_resid<double>(B, nb, B.resid);
+        }
         plan_chain_solve(B, maxpart, B.corr);
         plan_vec<float>(B, VEC_ADD, B.corr);
         plan_vec<double>(B, VEC_ADD, B.corr);
@@ -768,7 +781,7 @@ extern "C" int bss_batch_create(int32_t nsys, const int64_t *N, const int64_t *n
         // systems shorter than two chains run as one sequential chain (the
         // cheapest schedule; the batch supplies the parallelism).  Mixed: the
         // coarsest level is FP64, so every system is partitioned down to 2.
-        const long long chain = batch_chain_blocks(b->opt, (int)n[s]);
+        const long long chain = batch_chain_blocks(b->opt, (int)n[s], dtype);
         h->opt.plan = BSS_PLAN_AUTO;
         h->opt.target_partitions = (int)std::max<long long>(1, N[s] / chain);
         if (!b->mixed && N[s] < 2 * chain) h->opt.seq_cutoff = (int)std::max<long long>(1, N[s]);

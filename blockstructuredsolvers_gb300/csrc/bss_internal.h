@@ -96,6 +96,9 @@ ChainFactorArgs<Tin, T> make_factor_args(bss_handle *h, int l);
 template <class T>
 SolveArgs<T> make_solve_args(bss_handle *h, int l, int j0, int kc);
 
+// tuned plan for (n, dtype, precision), if the autotuner has one
+bool tuned_plan(int n, int dtype, int precision, bss_tune_entry *out);
+
 // asynchronous pieces of the mixed-precision solve (enqueue on h->ls; each
 // of begin/correct ends with the status copied to the pinned h->h_st)
 int mixed_begin(bss_handle *h);

@@ -299,6 +299,51 @@ int bss_server_get_stats(bss_server *s, bss_server_stats *stats);
 /* Clears the latency record and counters (not the resident factors). */
 int bss_server_reset_stats(bss_server *s);
 
+/* ---- CPU block Cholesky (host memory) ---------------------------------------
+ * Replaces initialize_cpu / factorize! / solve! of BlockTriDiagData_cpu
+ * (reference src/cpu.jl:12-50 over src/backbone_cpu.jl:5-33) with host C++:
+ * the sequential block recursion potrf('U') / trsm('L','U','T','N') /
+ * gemm('T','N') and its two sweeps.  Tensors are HOST memory in the same
+ * column-major layouts (A n x n x N, B n x n x (N-1), d n x k x N), zeroed
+ * at creation.  factorize leaves U_i in A_i's upper triangle and
+ * U_i^{-T} B_i in B_i, like the reference; a non-positive pivot returns
+ * BSS_ERR_NOT_SPD (the reference ignores potrf's info) and
+ * bss_cpu_failed_block names the block.  No GPU is used. */
+typedef struct bss_cpu_handle bss_cpu_handle;
+int bss_cpu_create(int64_t N, int64_t n, int64_t k, int32_t dtype, bss_cpu_handle **out);
+int bss_cpu_destroy(bss_cpu_handle *h);
+int bss_cpu_get_tensors(bss_cpu_handle *h, void **A, void **B, void **d);
+int bss_cpu_factorize(bss_cpu_handle *h);
+int bss_cpu_solve(bss_cpu_handle *h);
+int bss_cpu_failed_block(bss_cpu_handle *h, int64_t *block);
+
+/* ---- plan autotuner per (n, dtype, precision) ------------------------------
+ * No counterpart in the reference.  Tile shapes and CTA sizes are fixed per
+ * block-size class; the tuner picks the plan: finest-level partitions as a
+ * multiple of one wave of resident chain CTAs (wave_mult_x4 / 4), the
+ * sequential cutoff, and the batch chain length, by timing factorize+solve
+ * of a device-generated SPD system of N_probe blocks (0: 16384) and of a
+ * batch of 256 systems of 512 blocks.  Results go to a process-wide table
+ * that the planners consult whenever the caller leaves target_partitions,
+ * seq_cutoff or chain_blocks at 0 (so tuning changes the partitioning, and
+ * with it the rounding, of later handles).  Blocks while it runs (seconds). */
+typedef struct {
+    int32_t n, dtype, precision;
+    int32_t wave_mult_x4;   /* finest-level partitions = waves x 4 / 4 */
+    int32_t seq_cutoff;
+    int32_t chain_blocks;
+    double single_ms;       /* best factorize+solve time of the probe system */
+    double batch_ms;        /* best factorize+solve time of the probe batch  */
+} bss_tune_entry;
+
+int bss_autotune(int64_t n, int32_t dtype, int32_t precision, int64_t N_probe, bss_tune_entry *out);
+int bss_autotune_lookup(int64_t n, int32_t dtype, int32_t precision, bss_tune_entry *out);
+void bss_autotune_clear(void);
+/* text cache: one line per entry (n dtype precision wave_mult_x4 seq_cutoff
+ * chain_blocks single_ms batch_ms) */
+int bss_autotune_save(const char *path);
+int bss_autotune_load(const char *path);
+
 /* Number of CUDA kernels this library has launched in this process, over
  * all handles (no counterpart in the reference; benchmarks report it). */
 int64_t bss_kernel_launches(void);
