@@ -1124,6 +1124,151 @@ __device__ __forceinline__ void cta_nmul(const T *M1, const T *v1, const T *M2, 
     }
 }
 
+// Forms of the two products for blocks read straight from global memory
+// (the unstaged solve): the loads of a thread are independent and issued
+// together before their FMAs (so a warp waits for memory once per batch of
+// loads, not once per element), and every matrix element is used for all
+// right-hand-side columns of the pass.
+//
+// out(c, j) (+)= sign * sum_r M(r, c) v(r, j): a warp takes 4 columns; each
+// lane holds 4 rows x 4 columns of M (16 loads in flight) per 128-row slab.
+template <class T>
+__device__ __forceinline__ void cta_tmul_g(const T *M, const T *v, T *out, int n, int kc, T sign, bool accumulate)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int c0 = 4 * warp; c0 < n; c0 += 4 * nw) {
+        for (int j0 = 0; j0 < kc; j0 += 4) {
+            T s[4][4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int jj = 0; jj < 4; ++jj) s[q][jj] = T(0);
+            for (int rb = 0; rb < n; rb += 128) {
+                T m[4][4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int r = rb + lane + 32 * t;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        m[t][q] = (r < n && c0 + q < n) ? M[r + (size_t)(c0 + q) * n] : T(0);
+                }
+#pragma unroll
+                for (int jj = 0; jj < 4; ++jj) {
+                    if (j0 + jj >= kc) break;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const int r = rb + lane + 32 * t;
+                        const T vr = r < n ? v[r + (j0 + jj) * n] : T(0);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) s[q][jj] = fma(m[t][q], vr, s[q][jj]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int jj = 0; jj < 4; ++jj) s[q][jj] += __shfl_xor_sync(0xffffffffu, s[q][jj], o);
+            if (lane < 16) {
+                const int q = lane >> 2, jj = lane & 3;
+                T val = T(0);
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int b = 0; b < 4; ++b)
+                        if (a == q && b == jj) val = s[a][b];
+                if (c0 + q < n && j0 + jj < kc) {
+                    const int o = c0 + q + (j0 + jj) * n;
+                    out[o] = accumulate ? out[o] + sign * val : sign * val;
+                }
+            }
+        }
+    }
+}
+
+// out(r, j) = base(r, j) + sign * (sum_c M1(r, c) v1(c, j) [+ sum_c M2(r, c) v2(c, j)]):
+// a thread owns one row and up to 8 columns of the pass; blocks of 4
+// columns of M are loaded together.  With fewer rows than threads the
+// contraction is split over `parts` thread groups reduced through `red`
+// (parts x 8 x n elements).  Ends with a barrier.
+template <class T>
+__device__ __forceinline__ void cta_nmul_g(const T *M1, const T *v1, const T *M2, const T *v2, const T *base, T *out,
+                                           T sign, int n, int kc, T *red)
+{
+    int parts = (int)blockDim.x / n;
+    parts = parts < 1 ? 1 : (parts > 8 ? 8 : parts);
+    for (int j0 = 0; j0 < kc; j0 += 8) {
+        const int jn = kc - j0 < 8 ? kc - j0 : 8;
+        for (int w = threadIdx.x; w < parts * n; w += blockDim.x) {
+            const int part = w / n, r = w - part * n;
+            const int c0 = (part * n) / parts, c1 = ((part + 1) * n) / parts;
+            T acc[8];
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) acc[jj] = T(0);
+            for (int mi = 0; mi < 2; ++mi) {
+                const T *M = mi == 0 ? M1 : M2;
+                const T *v = mi == 0 ? v1 : v2;
+                if (!M) continue;
+                for (int c = c0; c < c1; c += 4) {
+                    T m[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) m[u] = (c + u < c1) ? M[r + (size_t)(c + u) * n] : T(0);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        if (c + u >= c1) break;
+#pragma unroll
+                        for (int jj = 0; jj < 8; ++jj)
+                            if (jj < jn) acc[jj] = fma(m[u], v[(c + u) + (j0 + jj) * n], acc[jj]);
+                    }
+                }
+            }
+            if (parts == 1) {
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj)
+                    if (jj < jn) {
+                        const int o = r + (j0 + jj) * n;
+                        out[o] = (base ? base[o] : T(0)) + sign * acc[jj];
+                    }
+            } else {
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj)
+                    if (jj < jn) red[(part * 8 + jj) * n + r] = acc[jj];
+            }
+        }
+        __syncthreads();
+        if (parts > 1) {
+            for (int o = threadIdx.x; o < n * jn; o += blockDim.x) {
+                const int jj = o / n, r = o - jj * n;
+                T sum = T(0);
+                for (int q = 0; q < parts; ++q) sum += red[(q * 8 + jj) * n + r];
+                const int oo = r + (j0 + jj) * n;
+                out[oo] = (base ? base[oo] : T(0)) + sign * sum;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+template <bool STAGED, class T>
+__device__ __forceinline__ void tmul(const T *M, const T *v, T *out, int n, int kc, T sign, bool accumulate)
+{
+    if constexpr (STAGED)
+        cta_tmul<T>(M, v, out, n, kc, sign, accumulate);
+    else
+        cta_tmul_g<T>(M, v, out, n, kc, sign, accumulate);
+}
+
+template <bool STAGED, class T>
+__device__ __forceinline__ void nmul(const T *M1, const T *v1, const T *M2, const T *v2, const T *base, T *out,
+                                     T sign, int n, int kc, T *red)
+{
+    if constexpr (STAGED)
+        cta_nmul<T>(M1, v1, M2, v2, base, out, sign, n, kc, red);
+    else
+        cta_nmul_g<T>(M1, v1, M2, v2, base, out, sign, n, kc, red);
+}
+
 template <class T>
 struct SolveArgs {
     const T *Af;   // V per block
@@ -1147,10 +1292,19 @@ struct SolveArgs {
 constexpr size_t SOLVE_SMEM_MAX = 220 * 1024;
 
 template <class T>
+__host__ __device__ constexpr int solve_red_elems(int n, int kc, bool staged)
+{
+    // staged products reduce n*kc partials (or one per thread); the
+    // global-read products up to 8 parts x 8 columns x n
+    return staged ? (n * kc > SOLVE_THREADS ? n * kc : SOLVE_THREADS)
+                  : (SOLVE_THREADS / n >= 2 ? (SOLVE_THREADS / n > 8 ? 8 : SOLVE_THREADS / n) * 8 * n : 0) +
+                        SOLVE_THREADS;
+}
+
+template <class T>
 __host__ __device__ constexpr size_t solve_smem_bytes(int n, int kc, bool staged = true)
 {
-    return (size_t)((staged ? 6 * n * n : 0) + 6 * n * kc + (n * kc > SOLVE_THREADS ? n * kc : SOLVE_THREADS)) *
-           sizeof(T);
+    return (size_t)((staged ? 6 * n * n : 0) + 6 * n * kc + solve_red_elems<T>(n, kc, staged)) * sizeof(T);
 }
 
 // the staged form whenever its double buffer fits for this column chunk
@@ -1234,12 +1388,12 @@ __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long
         const T *mW = STAGED ? cur + nn : g.Bf + (i - 1) * (long long)nn;
         const T *mY = STAGED ? cur + 2 * nn : g.Y + i * (long long)nn;
         if (i > first) {
-            cta_tmul(mW, sy, sr, n, kc, T(-1), true);
+            tmul<STAGED>(mW, sy, sr, n, kc, T(-1), true);
             __syncthreads();
         }
-        cta_tmul(mV, sr, sy, n, kc, T(1), false);
+        tmul<STAGED>(mV, sr, sy, n, kc, T(1), false);
         __syncthreads();
-        if (!seq) cta_tmul(mY, sy, sbL, n, kc, T(1), true);
+        if (!seq) tmul<STAGED>(mY, sy, sbL, n, kc, T(1), true);
         store_rhs(g.d, sy, i, n, g.k, g.j0, kc);
     }
     cp_async_wait_all();
@@ -1247,7 +1401,7 @@ __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long
     if (!seq) {
         const T *wl = STAGED ? buf + (((last + 1 - first) & 1) * 3 + 1) * nn  // W_last, prefetched in the last step
                              : g.Bf + last * (long long)nn;
-        cta_tmul(wl, sy, sbR, n, kc, T(1), false);
+        tmul<STAGED>(wl, sy, sbR, n, kc, T(1), false);
         __syncthreads();
         T *bp = g.bvec + p * 2 * (long long)nkc;
         for (int e = threadIdx.x; e < nkc; e += blockDim.x) {
@@ -1279,10 +1433,10 @@ __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long
         const T *mV = STAGED ? cur : g.Af + i * (long long)nn;
         const T *mW = STAGED ? cur + nn : g.Bf + i * (long long)nn;
         if (i < last) {
-            cta_nmul<T>(mW, sx, nullptr, nullptr, sr, sr, T(-1), n, kc, red);
+            nmul<STAGED, T>(mW, sx, nullptr, nullptr, sr, sr, T(-1), n, kc, red);
             __syncthreads();
         }
-        cta_nmul<T>(mV, sr, nullptr, nullptr, nullptr, sx, T(1), n, kc, red);
+        nmul<STAGED, T>(mV, sr, nullptr, nullptr, nullptr, sx, T(1), n, kc, red);
         __syncthreads();
         store_rhs(g.d, sx, i, n, g.k, g.j0, kc);
     }
@@ -1386,9 +1540,9 @@ __device__ __forceinline__ void chain_bwd_body(const SolveArgs<T> &g, const long
         const T *mV = STAGED ? cur : g.Af + i * (long long)nn;
         const T *mW = STAGED ? cur + nn : g.Bf + i * (long long)nn;
         const T *mY = STAGED ? cur + 2 * nn : g.Y + i * (long long)nn;
-        cta_nmul<T>(mY, sxL, mW, sxn, sz, sz, T(-1), n, kc, red);
+        nmul<STAGED, T>(mY, sxL, mW, sxn, sz, sz, T(-1), n, kc, red);
         __syncthreads();
-        cta_nmul<T>(mV, sz, nullptr, nullptr, nullptr, sxt, T(1), n, kc, red);
+        nmul<STAGED, T>(mV, sz, nullptr, nullptr, nullptr, sxt, T(1), n, kc, red);
         __syncthreads();
         for (int e = threadIdx.x; e < n * kc; e += blockDim.x) sxn[e] = sxt[e];
         store_rhs(g.d, sxt, i, n, g.k, g.j0, kc);
