@@ -43,7 +43,7 @@ EXPORTS = (
     "bss_server_release", "bss_server_get_stats", "bss_server_reset_stats",
     "bss_autotune", "bss_autotune_lookup", "bss_autotune_clear", "bss_autotune_save", "bss_autotune_load",
     "bss_cpu_create", "bss_cpu_destroy", "bss_cpu_get_tensors", "bss_cpu_factorize", "bss_cpu_solve",
-    "bss_cpu_failed_block",
+    "bss_cpu_failed_block", "bss_tc_selftest", "bss_diag_wide_occupancy",
 )
 
 
@@ -208,6 +208,8 @@ def load(path: str | None = None):
     L.bss_cpu_factorize.argtypes = [vp]
     L.bss_cpu_solve.argtypes = [vp]
     L.bss_cpu_failed_block.argtypes = [vp, ctypes.POINTER(i64)]
+    L.bss_tc_selftest.argtypes = [i64, ctypes.POINTER(ctypes.c_double)]
+    L.bss_diag_wide_occupancy.argtypes = [ctypes.POINTER(i64)]
     for name in EXPORTS:
         if name not in ("bss_default_options", "bss_last_error_string", "bss_version", "bss_kernel_launches",
                         "bss_server_default_options", "bss_autotune_clear"):

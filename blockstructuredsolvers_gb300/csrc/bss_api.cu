@@ -537,6 +537,7 @@ cudaError_t factor_any(bss_handle *h, int l)
 static int factorize_upto(bss_handle *h, int upto)
 {
     BSS_CUDA(cudaMemsetAsync(&h->st->bad_key, 0xFF, sizeof(unsigned long long), h->ls));
+    BSS_CUDA(cudaMemsetAsync(&h->st->tc_timeout, 0, sizeof(int), h->ls));
     const bool mixed = h->opt.precision == BSS_PRECISION_MIXED;
     if (mixed) {
         // ||T||_inf is folded into the first residual after this factorization
@@ -951,6 +952,8 @@ extern "C" int bss_synchronize(bss_handle *h)
         h->iters_total_seen = h->h_st->iters_total;
         h->sticky = h->h_st->done ? BSS_OK : BSS_ERR_NOT_CONVERGED;
     }
+    if (h->factored && h->h_st->tc_timeout)
+        return fail(BSS_ERR_TIMEOUT, "a bounded tensor-core wait expired during factorize; the factors are void");
     const unsigned long long key = h->h_st->bad_key;
     if (h->factored && key != ~0ULL) {
         h->info.failed_level = (int32_t)(key >> 40);

@@ -38,6 +38,7 @@ __global__ void batch_status_kernel(DevStatus *const *sts, int nsys, int mode)
         st->bad_key = ~0ULL;
         st->anorm = 0ULL;
         st->need_anorm = 1;
+        st->tc_timeout = 0;
     } else {
         st->dnorm = 0ULL;
         st->rnorm = 0ULL;
@@ -141,17 +142,17 @@ cudaError_t queue_factor_nb(const ChainFactorArgs<Tin, T> *descs, const WorkItem
     return cudaGetLastError();
 }
 
-template <class Tin, class T>
+template <class Tin, class T, bool TC>
 cudaError_t queue_factor_wide(const ChainFactorArgs<Tin, T> *descs, const WorkItem *items, int nitems, int *head,
                               int sms, cudaStream_t s)
 {
-    const size_t smem = wide_factor_smem<T>();
-    auto kern = wide_chain_factor_queue_kernel<Tin, T>;
+    const size_t smem = wide_factor_smem<T, TC>();
+    auto kern = wide_chain_factor_queue_kernel<Tin, T, TC>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    int per = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, WIDE_THREADS, smem);
-    int grid = std::max(1, std::min(nitems, sms * std::max(per, 1)));
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    const int per = ctas_per_sm(kern, WIDE_THREADS, smem);
+    int grid = std::max(1, std::min(nitems, sms * per));
     e = cudaMemsetAsync(head, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
     kern<<<grid, WIDE_THREADS, smem, s>>>(descs, items, nitems, head);
@@ -164,7 +165,9 @@ cudaError_t queue_factor(int nb, const ChainFactorArgs<Tin, T> *descs, const Wor
                          int sms, cudaStream_t s)
 {
     switch (nb) {
-    case WIDE_CLASS: return queue_factor_wide<Tin, T>(descs, items, nitems, head, sms, s);
+    case WIDE_CLASS: return queue_factor_wide<Tin, T, false>(descs, items, nitems, head, sms, s);
+    case WIDE_CLASS + 1: return queue_factor_wide<Tin, T, std::is_same<T, float>::value>(descs, items, nitems, head,
+                                                                                         sms, s);
     case 16: return queue_factor_nb<Tin, T, 16>(descs, items, nitems, head, sms, s);
     case 32: return queue_factor_nb<Tin, T, 32>(descs, items, nitems, head, sms, s);
     default: return queue_factor_nb<Tin, T, 64>(descs, items, nitems, head, sms, s);
@@ -217,7 +220,8 @@ template <class Tin, class T>
 void plan_factor_level(Builder &B, int level, bool coarsest)
 {
     bss_batch *b = B.b;
-    for (int nb : {16, 32, 64, (int)WIDE_CLASS}) {
+    // wide blocks: the tensor-core form (FP32, n <= 128) is its own launch class
+    for (int nb : {16, 32, 64, (int)WIDE_CLASS, (int)WIDE_CLASS + 1}) {
         std::vector<ChainFactorArgs<Tin, T>> descs;
         std::vector<WorkItem> items;
         std::vector<long long> len;
@@ -225,7 +229,9 @@ void plan_factor_level(Builder &B, int level, bool coarsest)
             bss_handle *h = b->sys[s];
             const int L = (int)h->levels.size();
             const int l = coarsest ? L - 1 : level;
-            if (nb_class(h->n) != nb || l >= L) continue;
+            int cls = nb_class(h->n);
+            if (cls == WIDE_CLASS && wide_uses_tc<T>((int)h->n)) cls = WIDE_CLASS + 1;
+            if (cls != nb || l >= L) continue;
             const Level &lv = h->levels[l];
             if (lv.seq != coarsest) continue;
             if ((lv.tin == F64) != std::is_same<Tin, double>::value || (lv.t == F64) != std::is_same<T, double>::value)
@@ -896,6 +902,8 @@ extern "C" int bss_batch_synchronize(bss_batch *b)
     for (int s = 0; s < b->nsys; ++s) {
         const DevStatus &st = b->h_gather[s];
         bss_info &inf = b->sys[s]->info;
+        if (b->factored && st.tc_timeout && rc == BSS_OK)
+            rc = fail(BSS_ERR_TIMEOUT, "a bounded tensor-core wait expired in system " + std::to_string(s));
         if (b->factored && st.bad_key != ~0ULL) {
             inf.failed_level = (int32_t)(st.bad_key >> 40);
             inf.failed_block = (int64_t)(st.bad_key & ((1ULL << 40) - 1));

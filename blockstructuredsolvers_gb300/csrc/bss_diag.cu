@@ -1,0 +1,119 @@
+// Diagnostic: one tensor-core product C = X^T Y (the wide kernel's
+// tcgen05 3xTF32 path) against an FP64 product of the same FP32 inputs.
+// No counterpart in the reference; used by the tests.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "bss_internal.h"
+
+using namespace bss;
+
+namespace {
+
+__global__ void diag_fill_kernel(float *X, float *Y, int n)
+{
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * n; e += gridDim.x * blockDim.x) {
+        unsigned x = (unsigned)e * 2654435761u + 12345u;
+        x ^= x >> 13;
+        x *= 0x5bd1e995u;
+        x ^= x >> 15;
+        X[e] = (float)((int)(x & 0xFFFF) - 32768) / 32768.0f;
+        unsigned y = (unsigned)e * 40503u + 977u;
+        y ^= y >> 11;
+        y *= 0x27d4eb2du;
+        y ^= y >> 15;
+        Y[e] = (float)((int)(y & 0xFFFF) - 32768) / 65536.0f + (e % (n + 1) == 0 ? 1.0f : 0.0f);
+    }
+}
+
+__global__ void diag_ref_kernel(const float *X, const float *Y, double *R, int n)
+{
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * n; e += gridDim.x * blockDim.x) {
+        const int i = e % n, j = e / n;
+        double s = 0.0;
+        for (int k = 0; k < n; ++k) s += (double)X[k + i * n] * (double)Y[k + j * n];
+        R[e] = s;
+    }
+}
+
+__global__ void __launch_bounds__(256) diag_tc_kernel(const float *X, const float *Y, float *C, int n, int *abort_out)
+{
+    extern __shared__ __align__(128) unsigned char smem_wide[];
+    unsigned char *tail = smem_wide + TC_NSTAGE * TC_STAGE_BYTES;
+    TcCtx tcc{};
+    tc_setup(tcc, reinterpret_cast<uint32_t *>(tail + 16), reinterpret_cast<uint64_t *>(tail), smem_wide,
+             reinterpret_cast<int *>(tail + 32));
+    tc_tn<float>(tcc, X, Y, n, smem_wide);
+    tc_store<float>(tcc, C, n, 1.f, (const float *)nullptr);
+    if (threadIdx.x == 0) *abort_out = *tcc.abort;
+    tc_teardown(tcc);
+}
+
+}  // namespace
+
+extern "C" int bss_tc_selftest(int64_t n, double *max_rel_err)
+{
+    if (n < 1 || n > 128 || !max_rel_err) return fail(BSS_ERR_ARG, "bss_tc_selftest: 1 <= n <= 128");
+    float *X = nullptr, *Y = nullptr, *C = nullptr;
+    double *R = nullptr;
+    int *ab = nullptr;
+    const size_t nn = (size_t)n * n;
+    BSS_CUDA(cudaMalloc((void **)&X, nn * 4));
+    BSS_CUDA(cudaMalloc((void **)&Y, nn * 4));
+    BSS_CUDA(cudaMalloc((void **)&C, nn * 4));
+    BSS_CUDA(cudaMalloc((void **)&R, nn * 8));
+    BSS_CUDA(cudaMalloc((void **)&ab, 4));
+    diag_fill_kernel<<<64, 256>>>(X, Y, (int)n);
+    diag_ref_kernel<<<64, 256>>>(X, Y, R, (int)n);
+    const int smem = TC_NSTAGE * TC_STAGE_BYTES + 128;
+    cudaError_t e = cudaFuncSetAttribute(diag_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) {
+        diag_tc_kernel<<<1, 256, smem>>>(X, Y, C, (int)n, ab);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    std::vector<float> hc(nn);
+    std::vector<double> hr(nn);
+    int abort_flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(hc.data(), C, nn * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(hr.data(), R, nn * 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&abort_flag, ab, 4, cudaMemcpyDeviceToHost);
+    cudaFree(X);
+    cudaFree(Y);
+    cudaFree(C);
+    cudaFree(R);
+    cudaFree(ab);
+    if (e != cudaSuccess) return cuda_fail(e, "bss_tc_selftest");
+    if (abort_flag) return fail(BSS_ERR_TIMEOUT, "tensor-core wait expired");
+    double mx = 0.0, md = 0.0;
+    for (size_t q = 0; q < nn; ++q) {
+        mx = std::max(mx, std::abs(hr[q]));
+        md = std::max(md, std::abs((double)hc[q] - hr[q]));
+    }
+    *max_rel_err = mx > 0 ? md / mx : md;
+    return BSS_OK;
+}
+
+// Diagnostic: the occupancy query the planner makes for the FP32-factor
+// wide kernel (tensor-core form): out[0..2] = error codes of the two
+// attribute calls and the query, out[3] = blocks per SM, out[4] = registers
+// per thread, out[5] = dynamic shared memory bytes
+extern "C" int bss_diag_wide_occupancy(int64_t *out)
+{
+    if (!out) return fail(BSS_ERR_ARG, "out is NULL");
+    auto kern = wide_chain_factor_kernel<double, float, true>;
+    const size_t smem = wide_factor_smem<float, true>();
+    out[0] = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    out[1] = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    int nblk = -1;
+    out[2] = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, kern, WIDE_THREADS, smem);
+    out[3] = nblk;
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, kern);
+    out[4] = fa.numRegs;
+    out[5] = (int64_t)smem;
+    return BSS_OK;
+}

@@ -39,6 +39,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
+#include "bss_tc.cuh"
+
 namespace bss {
 
 // ---------------------------------------------------------------------------
@@ -56,6 +60,8 @@ struct DevStatus {
     int need_anorm;   // the next residual also accumulates ||T||_inf
     int active;       // batch refinement: this system takes the pending correction
     unsigned long long iters_total;  // corrections over all device-loop solves (never reset)
+    int tc_timeout;   // a bounded tensor-core wait expired (the factorization is void)
+    int pad_;
 };
 
 __device__ __forceinline__ void record_bad_pivot(DevStatus *st, int level, long long block)
@@ -742,23 +748,38 @@ __device__ __forceinline__ void wide_tn(T (&acc)[4][4], const Tx *X, const Ty *Y
     }
 }
 
-template <class T>
+// shared memory of the wide kernel: four 64 x 64 tiles (sX, sY, sS, sV), the
+// pivot reciprocals and a flag; the TC form puts the tensor-core operand
+// stage first (128-byte aligned), the control words (mbarriers, TMEM
+// address, abort flag) after it, and overlays sX and sY on the stage (the
+// tile products of the Cholesky phase never overlap a tensor-core product)
+template <class T, bool TC>
 constexpr size_t wide_factor_smem()
 {
-    return (size_t)(4 * Geo<T, 64>::SLOT + WT) * sizeof(T) + 16;
+    return TC ? (size_t)TC_NSTAGE * TC_STAGE_BYTES + 128 + (size_t)(2 * Geo<T, 64>::SLOT + WT) * sizeof(T) + 16
+              : (size_t)(4 * Geo<T, 64>::SLOT + WT) * sizeof(T) + 16;
+}
+
+// tensor-core form of the wide kernel: FP32 chains of blocks up to 128
+template <class T>
+__host__ __device__ constexpr bool wide_uses_tc(int n)
+{
+    return std::is_same<T, float>::value && n <= 128;
 }
 
 constexpr int WIDE_THREADS = 256;
 
-template <class Tin, class T>
-__device__ __noinline__ void wide_chain_factor_body(const ChainFactorArgs<Tin, T> &g, const long long p)
+template <class Tin, class T, bool TC>
+__device__ __noinline__ void wide_chain_factor_body(const ChainFactorArgs<Tin, T> &g, const long long p, TcCtx &tcc)
 {
     constexpr int SLOT = Geo<T, 64>::SLOT;
     constexpr int LD = Geo<T, 64>::LD;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *sX = reinterpret_cast<T *>(smem_raw);
+    extern __shared__ __align__(128) unsigned char smem_wide[];
+    unsigned char *tc_stage = smem_wide;  // TC form only
+    static_assert(!TC || 2 * SLOT * sizeof(T) <= TC_STAGE_BYTES, "sX, sY overlay the tensor-core stage");
+    T *sX = reinterpret_cast<T *>(smem_wide);
     T *sY = sX + SLOT;
-    T *sS = sY + SLOT;
+    T *sS = TC ? reinterpret_cast<T *>(smem_wide + TC_NSTAGE * TC_STAGE_BYTES + 128) : sY + SLOT;
     T *sV = sS + SLOT;
     T *dinv = sV + SLOT;
     int *sflag = reinterpret_cast<int *>(dinv + WT);
@@ -789,6 +810,20 @@ __device__ __noinline__ void wide_chain_factor_body(const ChainFactorArgs<Tin, T
         T *Zg = seq ? nullptr : g.Y + i * nn;
         const T *Yp = seq ? nullptr : g.Y + (i - 1) * nn;
 
+        bool dead = false;  // TC form: a tensor-core wait expired
+        if constexpr (TC) {
+            if (t > 0) {
+                tc_tn<T>(tcc, Wp, Wp, n, tc_stage);
+                tc_store<Tin>(tcc, Vg, n, -1.f, Ag);  // V slot <- A_i - W^T W (whole block)
+                if (!seq) {
+                    tc_tn<T>(tcc, Wp, Yp, n, tc_stage);
+                    tc_store<T>(tcc, Zg, n, -1.f, (const T *)nullptr);
+                }
+            } else {
+                for (long long e = tid; e < nn; e += WIDE_THREADS) Vg[e] = (T)Ag[e];
+            }
+            dead = *tcc.abort != 0;
+        } else
         // S = A_i - W_{i-1}^T W_{i-1}, upper tiles (every thread rewrites only its own elements)
         for (int I = 0; I < NT; ++I)
             for (int J = I; J < NT; ++J) {
@@ -805,6 +840,7 @@ __device__ __noinline__ void wide_chain_factor_body(const ChainFactorArgs<Tin, T
             }
         if (!seq) {
             if (t > 0) {
+                if constexpr (!TC)
                 for (int I = 0; I < NT; ++I)
                     for (int J = 0; J < NT; ++J) {
                         T acc[4][4];
@@ -903,6 +939,27 @@ __device__ __noinline__ void wide_chain_factor_body(const ChainFactorArgs<Tin, T
         __syncthreads();
 
         // Y_i = V^T Z and W_i = V^T B_i in place, row tiles bottom-up
+        // (TC form: the whole product lands in tensor memory first)
+        if constexpr (TC) {
+            if (!dead && !seq) {
+                tc_tn<T>(tcc, Vg, Zg, n, tc_stage);
+                tc_store<T>(tcc, Zg, n, 1.f, (const T *)nullptr);
+            }
+            if (!dead && has_next) {
+                tc_tn<Tin>(tcc, Vg, g.B_in + i * nn, n, tc_stage);
+                tc_store<T>(tcc, g.B_f + i * nn, n, 1.f, (const T *)nullptr);
+            }
+            if (!dead && !seq) {
+                T *Cll = g.C + p * 3 * nn;
+                tc_tn<T>(tcc, Zg, Zg, n, tc_stage);
+                tc_store<T>(tcc, Cll, n, 1.f, t > 0 ? (const T *)Cll : (const T *)nullptr);
+            }
+            if (dead || *tcc.abort) {
+                if (tid == 0) atomicOr(&g.st->tc_timeout, 1);
+                return;
+            }
+            continue;
+        }
         if (!seq)
             for (int I = NT - 1; I >= 0; --I)
                 for (int J = 0; J < NT; ++J) {
@@ -948,6 +1005,14 @@ __device__ __noinline__ void wide_chain_factor_body(const ChainFactorArgs<Tin, T
         const T *Wl = g.B_f + last * nn;
         const T *Yl = g.Y + last * nn;
         T *Cp = g.C + p * 3 * nn;
+        if constexpr (TC) {
+            tc_tn<T>(tcc, Wl, Wl, n, tc_stage);
+            tc_store<T>(tcc, Cp + nn, n, 1.f, (const T *)nullptr);
+            tc_tn<T>(tcc, Yl, Wl, n, tc_stage);
+            tc_store<T>(tcc, Cp + 2 * nn, n, 1.f, (const T *)nullptr);
+            if (*tcc.abort && tid == 0) atomicOr(&g.st->tc_timeout, 1);
+            return;
+        }
         for (int I = 0; I < NT; ++I)
             for (int J = 0; J < NT; ++J) {
                 T acc[4][4];
@@ -961,18 +1026,42 @@ __device__ __noinline__ void wide_chain_factor_body(const ChainFactorArgs<Tin, T
     }
 }
 
-template <class Tin, class T>
-__global__ void __launch_bounds__(WIDE_THREADS) wide_chain_factor_kernel(ChainFactorArgs<Tin, T> g)
+// TC form: the CTA owns a 128-column TMEM accumulator and two mbarriers for
+// its lifetime (set up here, released before exit)
+template <bool TC>
+__device__ __forceinline__ void wide_tc_begin(TcCtx &tcc)
 {
-    wide_chain_factor_body<Tin, T>(g, blockIdx.x);
+    if constexpr (TC) {
+        extern __shared__ __align__(128) unsigned char smem_wide[];
+        unsigned char *tail = smem_wide + TC_NSTAGE * TC_STAGE_BYTES;  // 128 bytes of control words
+        tc_setup(tcc, reinterpret_cast<uint32_t *>(tail + 16), reinterpret_cast<uint64_t *>(tail), smem_wide,
+                 reinterpret_cast<int *>(tail + 32));
+    }
 }
 
-template <class Tin, class T>
-__global__ void __launch_bounds__(WIDE_THREADS)
+template <bool TC>
+__device__ __forceinline__ void wide_tc_end(const TcCtx &tcc)
+{
+    if constexpr (TC) tc_teardown(tcc);
+}
+
+template <class Tin, class T, bool TC>
+__global__ void __launch_bounds__(WIDE_THREADS, TC ? 2 : 1) wide_chain_factor_kernel(ChainFactorArgs<Tin, T> g)
+{
+    TcCtx tcc{};
+    wide_tc_begin<TC>(tcc);
+    wide_chain_factor_body<Tin, T, TC>(g, blockIdx.x, tcc);
+    wide_tc_end<TC>(tcc);
+}
+
+template <class Tin, class T, bool TC>
+__global__ void __launch_bounds__(WIDE_THREADS, TC ? 2 : 1)
     wide_chain_factor_queue_kernel(const ChainFactorArgs<Tin, T> *__restrict__ descs,
                                    const WorkItem *__restrict__ items, int nitems, int *head)
 {
     __shared__ int cur;
+    TcCtx tcc{};
+    wide_tc_begin<TC>(tcc);
     for (;;) {
         if (threadIdx.x == 0) cur = atomicAdd(head, 1);
         __syncthreads();
@@ -981,9 +1070,13 @@ __global__ void __launch_bounds__(WIDE_THREADS)
         if (it >= nitems) break;
         const WorkItem w = items[it];
         const ChainFactorArgs<Tin, T> g = descs[w.desc];
-        wide_chain_factor_body<Tin, T>(g, w.p);
+        wide_chain_factor_body<Tin, T, TC>(g, w.p, tcc);
         __syncthreads();
+        if constexpr (TC) {
+            if (*tcc.abort) break;  // uniform: set before the body's last barrier
+        }
     }
+    wide_tc_end<TC>(tcc);
 }
 
 // ---------------------------------------------------------------------------
@@ -1188,7 +1281,7 @@ __device__ __forceinline__ void cta_tmul_g(const T *M, const T *v, T *out, int n
 }
 
 // out(r, j) = base(r, j) + sign * (sum_c M1(r, c) v1(c, j) [+ sum_c M2(r, c) v2(c, j)]):
-// a thread owns one row and up to 8 columns of the pass; blocks of 4
+// a thread owns one row and up to 8 columns of the pass; blocks of 16
 // columns of M are loaded together.  With fewer rows than threads the
 // contraction is split over `parts` thread groups reduced through `red`
 // (parts x 8 x n elements).  Ends with a barrier.
@@ -1210,12 +1303,12 @@ __device__ __forceinline__ void cta_nmul_g(const T *M1, const T *v1, const T *M2
                 const T *M = mi == 0 ? M1 : M2;
                 const T *v = mi == 0 ? v1 : v2;
                 if (!M) continue;
-                for (int c = c0; c < c1; c += 4) {
-                    T m[4];
+                for (int c = c0; c < c1; c += 16) {
+                    T m[16];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) m[u] = (c + u < c1) ? M[r + (size_t)(c + u) * n] : T(0);
+                    for (int u = 0; u < 16; ++u) m[u] = (c + u < c1) ? M[r + (size_t)(c + u) * n] : T(0);
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
+                    for (int u = 0; u < 16; ++u) {
                         if (c + u >= c1) break;
 #pragma unroll
                         for (int jj = 0; jj < 8; ++jj)

@@ -54,6 +54,28 @@ cudaError_t launch_init_identity(T *A, long long first_blk, long long last_blk, 
 
 int solve_kc_max(int n, int k, int elem_bytes);
 
+// resident CTAs per SM of a kernel: the larger of the occupancy query and
+// the count from its registers and shared memory (the query reports one CTA
+// per SM for the tensor-core wide kernel although its resources admit two)
+template <class K>
+inline int ctas_per_sm(K kern, int threads, size_t smem)
+{
+    int nblk = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, kern, threads, smem) != cudaSuccess) nblk = 1;
+    int dev = 0, smem_sm = 0, reserved = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, kern) == cudaSuccess && fa.numRegs > 0) {
+        const int by_smem = smem_sm / (int)(smem + fa.sharedSizeBytes + reserved);
+        const int by_regs = 65536 / (fa.numRegs * threads);
+        const int by_res = by_smem < by_regs ? by_smem : by_regs;
+        if (by_res > nblk) nblk = by_res;
+    }
+    return nblk > 0 ? nblk : 1;
+}
+
 // message returned by bss_last_error_string() on this host thread
 void set_last_error(const std::string &msg);
 

@@ -26,17 +26,27 @@ static cudaError_t chain_factor_nb(const ChainFactorArgs<Tin, T> &a, cudaStream_
     return cudaGetLastError();
 }
 
-template <class Tin, class T>
-static cudaError_t wide_chain_factor(const ChainFactorArgs<Tin, T> &a, cudaStream_t s)
+template <class Tin, class T, bool TC>
+static cudaError_t wide_chain_factor_tc(const ChainFactorArgs<Tin, T> &a, cudaStream_t s)
 {
-    const size_t smem = wide_factor_smem<T>();
-    auto kern = wide_chain_factor_kernel<Tin, T>;
+    const size_t smem = wide_factor_smem<T, TC>();
+    auto kern = wide_chain_factor_kernel<Tin, T, TC>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     const unsigned grid = a.seq ? 1u : (unsigned)a.Q;
     kern<<<grid, WIDE_THREADS, smem, s>>>(a);
     count_launch();
     return cudaGetLastError();
+}
+
+template <class Tin, class T>
+static cudaError_t wide_chain_factor(const ChainFactorArgs<Tin, T> &a, cudaStream_t s)
+{
+    if constexpr (std::is_same<T, float>::value) {
+        if (wide_uses_tc<T>(a.n)) return wide_chain_factor_tc<Tin, T, true>(a, s);
+    }
+    return wide_chain_factor_tc<Tin, T, false>(a, s);
 }
 
 template <class Tin, class T>
@@ -62,15 +72,15 @@ static int ctas_nb()
     return nblk > 0 ? nblk : 1;
 }
 
-template <class Tin, class T>
-static int wide_ctas()
+template <class Tin, class T, bool TC>
+static int wide_ctas_tc()
 {
-    const size_t smem = wide_factor_smem<T>();
-    auto kern = wide_chain_factor_kernel<Tin, T>;
+    const size_t smem = wide_factor_smem<T, TC>();
+    auto kern = wide_chain_factor_kernel<Tin, T, TC>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
-    int nblk = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, kern, WIDE_THREADS, smem) != cudaSuccess) return 1;
-    return nblk > 0 ? nblk : 1;
+    // ask for the whole unified L1/shared array as shared memory
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    return ctas_per_sm(kern, WIDE_THREADS, smem);
 }
 
 template <class Tin, class T>
@@ -80,7 +90,11 @@ int chain_factor_ctas_per_sm(int n)
     case 16: return ctas_nb<Tin, T, 16>();
     case 32: return ctas_nb<Tin, T, 32>();
     case 64: return ctas_nb<Tin, T, 64>();
-    case WIDE_CLASS: return wide_ctas<Tin, T>();
+    case WIDE_CLASS:
+        if constexpr (std::is_same<T, float>::value) {
+            if (wide_uses_tc<T>(n)) return wide_ctas_tc<Tin, T, true>();
+        }
+        return wide_ctas_tc<Tin, T, false>();
     default: return 1;
     }
 }

@@ -373,6 +373,11 @@ int advance_request(bss_server *S, Request *r)
     bss_handle *h = f->h;
     cudaStream_t st = S->streams[f->slot];
     const DevStatus &hs = *h->h_st;
+    if (hs.tc_timeout && r->kind != RQ_RHS) {
+        r->status = BSS_ERR_TIMEOUT;
+        r->phase = PH_DONE;
+        return BSS_OK;
+    }
     if (r->phase == PH_FINISH) {
         if (hs.bad_key != ~0ULL && r->kind != RQ_RHS) r->status = BSS_ERR_NOT_SPD;
         r->phase = PH_DONE;

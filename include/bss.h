@@ -344,6 +344,18 @@ void bss_autotune_clear(void);
 int bss_autotune_save(const char *path);
 int bss_autotune_load(const char *path);
 
+/* Diagnostic (no counterpart in the reference): one tensor-core product
+ * C = X^T Y of n x n FP32 blocks (n <= 128) through the wide kernel's
+ * tcgen05 3xTF32 path, compared with an FP64 product of the same inputs;
+ * *max_rel_err = max |C - C64| / max |C64|.  Allocates and synchronises. */
+int bss_tc_selftest(int64_t n, double *max_rel_err);
+
+/* Diagnostic (no counterpart in the reference): the planner's occupancy
+ * query for the tensor-core wide kernel.  out[0..5]: the CUDA error codes of
+ * the two attribute calls and of the query, blocks per SM, registers per
+ * thread, dynamic shared memory bytes. */
+int bss_diag_wide_occupancy(int64_t *out);
+
 /* Number of CUDA kernels this library has launched in this process, over
  * all handles (no counterpart in the reference; benchmarks report it). */
 int64_t bss_kernel_launches(void);
