@@ -306,38 +306,60 @@ def run_ours(args):
                                "note": "FP32 accuracy only; not a rel-resid <= 1e-12 result"}
 
     # ---- e2e through the public API with host buffers ----------------------
+    # A stream of requests, each: pinned host A, B, d -> device, factorize!,
+    # solve!, x -> pinned host.  Two handles on two CUDA streams take
+    # alternate requests (the double buffering a serving caller uses), so
+    # one request's copies overlap the other's compute; every request still
+    # pays its own H2D and D2H inside the timed region.  The one-handle
+    # serial figure is reported beside it.
     e2e = None
     if not args.quick:
         # host copies in the handle's storage order: (N, c, r) C-order == column-major blocks
         Ah = A.permute(2, 1, 0).contiguous().cpu().pin_memory()
         Bh = B.permute(2, 1, 0).contiguous().cpu().pin_memory()
         dh = d.permute(2, 1, 0).contiguous().cpu().pin_memory()
-        xh = torch.empty_like(dh).pin_memory()
-        data = bss.initialize_batched(N_BLK, N_SZ, torch.float64, k=K_RHS, precision="mixed")
-        At = data.A_tensor[:, :, :N_BLK].permute(2, 1, 0)  # contiguous (N, c, r) views
-        Bt = data.B_tensor[:, :, :N_BLK - 1].permute(2, 1, 0)
-        dt = data.d_tensor[:, :, :N_BLK].permute(2, 1, 0)
-        ne = max(3, args.steps // 4)
+        streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+        slots = []
+        for st in streams:
+            with torch.cuda.stream(st):
+                data = bss.initialize_batched(N_BLK, N_SZ, torch.float64, k=K_RHS, precision="mixed", stream=st)
+            slots.append((st, data, data.A_tensor[:, :, :N_BLK].permute(2, 1, 0),
+                          data.B_tensor[:, :, :N_BLK - 1].permute(2, 1, 0),
+                          data.d_tensor[:, :, :N_BLK].permute(2, 1, 0), torch.empty_like(dh).pin_memory()))
+        ne = max(4, args.steps // 4)
 
-        def e2e_step():
-            At.copy_(Ah, non_blocking=True)
-            Bt.copy_(Bh, non_blocking=True)
-            dt.copy_(dh, non_blocking=True)
-            bss.factorize_(data)
-            bss.solve_(data)
-            xh.copy_(dt, non_blocking=True)
+        def e2e_step(slot):
+            st, data, At, Bt, dt, xh = slot
+            with torch.cuda.stream(st):
+                At.copy_(Ah, non_blocking=True)
+                Bt.copy_(Bh, non_blocking=True)
+                dt.copy_(dh, non_blocking=True)
+                bss.factorize_(data)
+                bss.solve_(data)
+                xh.copy_(dt, non_blocking=True)
 
-        e2e_step()
+        for slot in slots:  # first calls run eagerly and capture the graphs
+            for _ in range(2):
+                e2e_step(slot)
         torch.cuda.synchronize()
         tt0 = time.perf_counter()
-        for _ in range(ne):
-            e2e_step()
+        for i in range(ne):
+            e2e_step(slots[i % 2])
         torch.cuda.synchronize()
         te = time.perf_counter() - tt0
+        tt0 = time.perf_counter()
+        for i in range(max(3, ne // 2)):
+            e2e_step(slots[0])
+        torch.cuda.synchronize()
+        te1 = (time.perf_counter() - tt0) / max(3, ne // 2)
+        x_e2e = slots[0][5].permute(2, 1, 0)  # (n, k, N) view of the last x
+        rr_e2e = rel_residual_dev(A, B, x_e2e.to(dev), d)
         bi = (Ah.numel() + Bh.numel() + dh.numel()) * 8
-        bo = xh.numel() * 8
-        e2e = {"value": world * ne / te, "unit": "solves/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo}
-        del data
+        bo = slots[0][5].numel() * 8
+        e2e = {"value": world * ne / te, "unit": "solves/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
+               "mode": "two handles on two streams, alternate requests, copies inside the timed region",
+               "serial_one_handle": world / te1, "rel_residual_last_x": rr_e2e}
+        del slots
 
     # ---- roofline of the dominant kernel ----------------------------------
     peaks = {}
