@@ -52,10 +52,8 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from blockstructuredsolvers_gb300 import replicas
+    return replicas.rank_env()
 
 
 # --------------------------------------------------------------------------
@@ -281,10 +279,8 @@ def run_ours(args):
     launches_per_step = None
     # the warmup steps launched too: count per step from the total
     launches_per_step = launches / max(args.steps + args.warmup, 1)
-    if world > 1:
-        t = torch.tensor([secs], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        secs = t.item()
+    from blockstructuredsolvers_gb300 import replicas
+    secs = replicas.reduce_max(secs)  # the slowest replica's time
     value = world * args.steps / secs
 
     extra = {}
