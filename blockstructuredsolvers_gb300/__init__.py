@@ -27,6 +27,7 @@ __all__ = [
     "BlockTriDiagData_batched", "BlockTriDiagData_seq", "initialize_batched", "initialize_seq",
     "factorize_", "solve_", "factorize", "solve", "synchronize", "get_info", "residual",
     "plan_reference", "BSSError", "NotSPDError", "MultiSystemBatch", "initialize_multi", "Server", "kf_build", "BlockTriDiagData_cpu", "initialize_cpu",
+    "ReferenceAlgorithmData", "initialize_reference_algorithm",
     "autotune", "autotune_lookup", "autotune_save", "autotune_load", "autotune_clear",
 ]
 
@@ -175,6 +176,62 @@ def initialize_seq(N: int, n: int, T=None, M=None, *, k: int = 1, stream=None) -
     return BlockTriDiagData_seq(_Handle(h.value), tdt, int(N))
 
 
+class _RefHandle:
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                _lib.load().bss_refalgo_destroy(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+
+class ReferenceAlgorithmData:
+    """The reference's batched GPU algorithm restated over cuSOLVER/cuBLAS
+    (bss_refalgo_*), for comparison: same tensors as BlockTriDiagData_batched
+    (A_tensor, B_tensor, d_tensor column-major views of N_use blocks)."""
+
+    def __init__(self, handle: _RefHandle, torch_dtype):
+        torch = _torch()
+        L = _lib.load()
+        self._h = handle
+        N, n, k = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _lib.check(L.bss_refalgo_get_dims(handle.ptr, ctypes.byref(N), ctypes.byref(n), ctypes.byref(k)))
+        A, B, d = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        _lib.check(L.bss_refalgo_get_tensors(handle.ptr, ctypes.byref(A), ctypes.byref(B), ctypes.byref(d)))
+        self.N, self.n, self.k, self.dtype = N.value, n.value, k.value, torch_dtype
+        es = 8 if torch_dtype == torch.float64 else 4
+        ts = "<f8" if es == 8 else "<f4"
+        nn = self.n * self.n
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self.A_tensor = torch.as_tensor(
+            _DevView(A.value, (self.n, self.n, self.N), (es, es * self.n, es * nn), ts, handle), device=dev)
+        self.B_tensor = torch.as_tensor(
+            _DevView(B.value, (self.n, self.n, max(self.N - 1, 0)), (es, es * self.n, es * nn), ts, handle),
+            device=dev)
+        self.d_tensor = torch.as_tensor(
+            _DevView(d.value, (self.n, self.k, self.N), (es, es * self.n, es * self.n * self.k), ts, handle),
+            device=dev)
+
+    @property
+    def handle(self):
+        return self._h.ptr
+
+
+def initialize_reference_algorithm(N: int, n: int, T=None, *, k: int = 1, stream=None) -> ReferenceAlgorithmData:
+    """The reference's own algorithm (src/gpu_batched.jl over batched
+    cuSOLVER/cuBLAS) on this GPU, for timing comparisons."""
+    torch = _torch()
+    code, tdt = _dtype_code(torch.float64 if T is None else T)
+    h = ctypes.c_void_p()
+    torch.cuda.current_device()
+    _lib.check(_lib.load().bss_refalgo_create(int(N), int(n), int(k), code, _stream_ptr(stream), ctypes.byref(h)))
+    return ReferenceAlgorithmData(_RefHandle(h.value), tdt)
+
+
 class _CpuHandle:
     def __init__(self, ptr):
         self.ptr = ptr
@@ -244,6 +301,9 @@ def factorize_(data, check: bool = False) -> None:
     if isinstance(data, BlockTriDiagData_cpu):
         _lib.check(_lib.load().bss_cpu_factorize(data.handle))
         return
+    if isinstance(data, ReferenceAlgorithmData):
+        _lib.check(_lib.load().bss_refalgo_factorize(data.handle))
+        return
     _lib.check(_lib.load().bss_factorize(data.handle))
     if check:
         synchronize(data)
@@ -254,6 +314,9 @@ def solve_(data, check: bool = False) -> None:
     src/cpu.jl:42-50): d_tensor <- A^{-1} d_tensor."""
     if isinstance(data, BlockTriDiagData_cpu):
         _lib.check(_lib.load().bss_cpu_solve(data.handle))
+        return
+    if isinstance(data, ReferenceAlgorithmData):
+        _lib.check(_lib.load().bss_refalgo_solve(data.handle))
         return
     _lib.check(_lib.load().bss_solve(data.handle))
     if check:

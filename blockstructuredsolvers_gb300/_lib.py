@@ -44,6 +44,8 @@ EXPORTS = (
     "bss_autotune", "bss_autotune_lookup", "bss_autotune_clear", "bss_autotune_save", "bss_autotune_load",
     "bss_cpu_create", "bss_cpu_destroy", "bss_cpu_get_tensors", "bss_cpu_factorize", "bss_cpu_solve",
     "bss_cpu_failed_block", "bss_tc_selftest", "bss_diag_wide_occupancy",
+    "bss_refalgo_create", "bss_refalgo_destroy", "bss_refalgo_get_tensors", "bss_refalgo_get_dims",
+    "bss_refalgo_factorize", "bss_refalgo_solve",
 )
 
 
@@ -210,6 +212,12 @@ def load(path: str | None = None):
     L.bss_cpu_failed_block.argtypes = [vp, ctypes.POINTER(i64)]
     L.bss_tc_selftest.argtypes = [i64, ctypes.POINTER(ctypes.c_double)]
     L.bss_diag_wide_occupancy.argtypes = [ctypes.POINTER(i64)]
+    L.bss_refalgo_create.argtypes = [i64, i64, i64, i32, vp, ctypes.POINTER(vp)]
+    L.bss_refalgo_destroy.argtypes = [vp]
+    L.bss_refalgo_get_tensors.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    L.bss_refalgo_get_dims.argtypes = [vp, ctypes.POINTER(i64), ctypes.POINTER(i64), ctypes.POINTER(i64)]
+    L.bss_refalgo_factorize.argtypes = [vp]
+    L.bss_refalgo_solve.argtypes = [vp]
     for name in EXPORTS:
         if name not in ("bss_default_options", "bss_last_error_string", "bss_version", "bss_kernel_launches",
                         "bss_server_default_options", "bss_autotune_clear"):

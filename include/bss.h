@@ -344,6 +344,25 @@ void bss_autotune_clear(void);
 int bss_autotune_save(const char *path);
 int bss_autotune_load(const char *path);
 
+/* ---- the reference's algorithm on this GPU (comparison) ---------------------
+ * A restatement of factorize!/solve! of BlockTriDiagData_batched
+ * (src/gpu_batched.jl:184-258) over the same batched cuSOLVER/cuBLAS calls
+ * (potrfBatched, trsmBatched, gemmBatched; src/backbone_cuda.jl:14-184), the
+ * same n x 2n fill F = T^{-1} G and M_2n Schur products, the reference
+ * planner's padded size and levels, and a sequential coarsest level.  For
+ * timing the reference's own GPU algorithm beside this library's kernels;
+ * it is not a path of bss_create_batched.  Tensors (device, column-major,
+ * N_use blocks, identity padding) as for bss_create_batched; factorize
+ * leaves the reference's factors in A/B; solve overwrites d.  Asynchronous
+ * on `stream`; pivot failures are not checked (as in the reference). */
+typedef struct bss_refalgo bss_refalgo;
+int bss_refalgo_create(int64_t N, int64_t n, int64_t k, int32_t dtype, void *stream, bss_refalgo **out);
+int bss_refalgo_destroy(bss_refalgo *h);
+int bss_refalgo_get_tensors(bss_refalgo *h, void **A, void **B, void **d);
+int bss_refalgo_get_dims(bss_refalgo *h, int64_t *N, int64_t *n, int64_t *k);
+int bss_refalgo_factorize(bss_refalgo *h);
+int bss_refalgo_solve(bss_refalgo *h);
+
 /* Diagnostic (no counterpart in the reference): one tensor-core product
  * C = X^T Y of n x n FP32 blocks (n <= 128) through the wide kernel's
  * tcgen05 3xTF32 path, compared with an FP64 product of the same inputs;
