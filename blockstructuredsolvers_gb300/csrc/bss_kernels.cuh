@@ -1250,6 +1250,7 @@ __device__ __forceinline__ void cta_tmul_g(const T *M, const T *v, T *out, int n
                     if (j0 + jj >= kc) break;
 #pragma unroll
                     for (int t = 0; t < 4; ++t) {
+                        if (rb + 32 * t >= n) break;  // warp-uniform: no FMAs on padding rows
                         const int r = rb + lane + 32 * t;
                         const T vr = r < n ? v[r + (j0 + jj) * n] : T(0);
 #pragma unroll
@@ -1343,10 +1344,16 @@ __device__ __forceinline__ void cta_nmul_g(const T *M1, const T *v1, const T *M2
     }
 }
 
+// Staged blocks: the transpose product takes the register-blocked form when
+// there are several right-hand-side columns (every matrix element reused
+// across them; lanes run along rows, conflict-free on shared memory, no
+// scratch), the one-column form otherwise; the normal product keeps its
+// staged form.  Blocks read from global memory take the register-blocked
+// forms.
 template <bool STAGED, class T>
 __device__ __forceinline__ void tmul(const T *M, const T *v, T *out, int n, int kc, T sign, bool accumulate)
 {
-    if constexpr (STAGED)
+    if (STAGED && kc == 1)
         cta_tmul<T>(M, v, out, n, kc, sign, accumulate);
     else
         cta_tmul_g<T>(M, v, out, n, kc, sign, accumulate);
@@ -1387,11 +1394,11 @@ constexpr size_t SOLVE_SMEM_MAX = 220 * 1024;
 template <class T>
 __host__ __device__ constexpr int solve_red_elems(int n, int kc, bool staged)
 {
-    // staged products reduce n*kc partials (or one per thread); the
-    // global-read products up to 8 parts x 8 columns x n
+    // the staged normal product reduces n*kc partials (or one per thread);
+    // the register-blocked one up to 8 parts x 8 columns x n
     return staged ? (n * kc > SOLVE_THREADS ? n * kc : SOLVE_THREADS)
-                  : (SOLVE_THREADS / n >= 2 ? (SOLVE_THREADS / n > 8 ? 8 : SOLVE_THREADS / n) * 8 * n : 0) +
-                        SOLVE_THREADS;
+                               : (SOLVE_THREADS / n >= 2 ? (SOLVE_THREADS / n > 8 ? 8 : SOLVE_THREADS / n) * 8 * n : 0) +
+                                     SOLVE_THREADS;
 }
 
 template <class T>
