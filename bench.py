@@ -317,6 +317,80 @@ def time_reference_algorithm(bss, A, B, d, reps=3):
             "what": "reference gpu_batched.jl algorithm over batched cuSOLVER/cuBLAS (FP64), restated in C++"}
 
 
+def hbm_peak():
+    """(GB/s, "measured" | "fallback"): the measured HBM copy bandwidth of
+    MEASURED_PEAKS.json, else the fallback 6.8 TB/s."""
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs")
+    return (hbm, "measured") if hbm else (6800.0, "fallback")
+
+
+def time_sparse_cholesky(bss, A, B, d, hbm_gbs):
+    """The reference's sparse comparison (benchmark/benchmark_gpu.jl:75-117:
+    analysis, factorization and solve of the assembled CSR matrix with a
+    sparse direct solver) in FP64 on the same system.  cuDSS is not in this
+    toolkit: cuSOLVER's GPU sparse Cholesky (csrchol*) stands in.  Each phase
+    runs once (seconds at this size), timed on the host around a
+    synchronize.  The CSR assembly kernel alone (bss_csr_assemble,
+    construct_block_tridiagonal of benchmark/utils.jl:59-103) is timed with
+    CUDA events over 5 launches (inputs and outputs larger than L2) against
+    the HBM copy peak."""
+    import ctypes
+    import torch
+    from blockstructuredsolvers_gb300 import _lib
+    n, _, N = A.shape
+    k = d.shape[1]
+    L = _lib.load()
+    nnz = int(L.bss_csr_nnz(N, n))
+    dev = A.device
+    crow = torch.empty(N * n + 1, dtype=torch.int32, device=dev)
+    col = torch.empty(nnz, dtype=torch.int32, device=dev)
+    val = torch.empty(nnz, dtype=torch.float64, device=dev)
+    Ac = A.permute(2, 1, 0).contiguous()   # (N, c, r): column-major blocks
+    Bc = B.permute(2, 1, 0).contiguous()
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(int(stream.cuda_stream))
+    ms = []
+    for r in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _lib.check(L.bss_csr_assemble(N, n, _lib.BSS_F64, ctypes.c_void_p(Ac.data_ptr()),
+                                      ctypes.c_void_p(Bc.data_ptr()), ctypes.c_void_p(crow.data_ptr()),
+                                      ctypes.c_void_p(col.data_ptr()), ctypes.c_void_p(val.data_ptr()), sp))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if r > 0:
+            ms.append(e0.elapsed_time(e1))
+    asm_ms = statistics.median(ms)
+    asm_bytes = 8 * n * n * (2 * N - 1) + 12 * nnz + 4 * (N * n + 1)
+    del crow, col, val, Ac, Bc
+    data = bss.initialize_sparse_cholesky(N, n, torch.float64, k=k)
+    data.A_tensor.copy_(A)
+    data.B_tensor.copy_(B)
+    data.d_tensor.copy_(d)
+    torch.cuda.synchronize()
+    t = {}
+    for ph, fn in (("analysis", bss.analyze_), ("factorization", bss.factorize_), ("solve", bss.solve_)):
+        t0 = time.perf_counter()
+        fn(data)
+        torch.cuda.synchronize()
+        t[ph] = (time.perf_counter() - t0) * 1e3
+    rr = rel_residual_dev(A, B, data.d_tensor, d)
+    del data
+    torch.cuda.empty_cache()
+    return {"solves_per_s": 1e3 / (t["factorization"] + t["solve"]), "analysis_ms": t["analysis"],
+            "factor_ms": t["factorization"], "solve_ms": t["solve"], "rel_residual": rr, "nnz": nnz,
+            "what": "assembled CSR matrix (construct_block_tridiagonal) on cuSOLVER's GPU sparse Cholesky "
+                    "(FP64), standing in for the reference's cuDSS comparison; cuDSS is not in this toolkit",
+            "csr_assembly": {"ms": asm_ms, "bytes": asm_bytes, "gbs": asm_bytes / asm_ms / 1e6,
+                             "frac_of_measured_hbm": asm_bytes / asm_ms / 1e6 / hbm_gbs}}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -364,6 +438,7 @@ def run_ours(args):
         del d32
         n64 = max(3, args.steps // 4)
         extra["reference_algorithm_gpu"] = time_reference_algorithm(bss, A, B, d)
+        extra["sparse_cholesky_gpu"] = time_sparse_cholesky(bss, A, B, d, hbm_peak()[0])
         extra["k16"] = run_k16(bss, A, B, dev)
         extra["plain_fp64"] = {"solves_per_s": n64 / s64, "factor_ms": statistics.median(f64),
                                "solve_ms": statistics.median(so64), "rel_residual": rr64,
@@ -429,15 +504,7 @@ def run_ours(args):
         del slots
 
     # ---- roofline of the dominant kernel ----------------------------------
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except Exception:
-        pass
-    hbm = peaks.get("hbm_gbs")
-    peak_kind = "measured" if hbm else "fallback"
-    hbm = hbm or 6800.0
+    hbm, peak_kind = hbm_peak()
     roof = roofline_chain_factor(bss, A, B, d, hbm, peak_kind)
 
     cpu_base = None

@@ -28,6 +28,7 @@ __all__ = [
     "factorize_", "solve_", "factorize", "solve", "synchronize", "get_info", "residual",
     "plan_reference", "BSSError", "NotSPDError", "MultiSystemBatch", "initialize_multi", "Server", "kf_build", "BlockTriDiagData_cpu", "initialize_cpu",
     "ReferenceAlgorithmData", "initialize_reference_algorithm",
+    "construct_block_tridiagonal", "SparseCholeskyData", "initialize_sparse_cholesky", "analyze_",
     "autotune", "autotune_lookup", "autotune_save", "autotune_load", "autotune_clear",
 ]
 
@@ -232,6 +233,134 @@ def initialize_reference_algorithm(N: int, n: int, T=None, *, k: int = 1, stream
     return ReferenceAlgorithmData(_RefHandle(h.value), tdt)
 
 
+def _blocks_colmajor(X, n, count):
+    """Device tensor (n, n, count) whose blocks are column-major in memory:
+    element (r, c, i) at i n^2 + c n + r (a copy only if X is laid out
+    otherwise)."""
+    if tuple(X.shape) != (n, n, count):
+        raise ValueError(f"expected blocks of shape ({n}, {n}, {count}), got {tuple(X.shape)}")
+    if count > 0 and tuple(X.stride()) != (1, n, n * n):
+        X = X.permute(2, 1, 0).contiguous().permute(2, 1, 0)
+    return X
+
+
+def construct_block_tridiagonal(A_tensor, B_tensor, d_tensor=None, *, stream=None):
+    """construct_block_tridiagonal(A_list, B_list, d_list)
+    (benchmark/utils.jl:59-103) on the device.
+
+    A_tensor (n x n x N) and B_tensor (n x n x (N-1)) are CUDA tensors of the
+    blocks (A_tensor[:, :, i] = A_i).  Returns ``(M, d_vec)``: M the
+    (N n) x (N n) matrix with A_i on the diagonal, B_i at block (i, i+1) and
+    B_i^T at block (i+1, i) as a torch sparse CSR tensor with int32 indices,
+    every entry of every block stored and the values copied bit for bit
+    (bss_csr_assemble); d_vec = vcat(d_list...), the (N n) x k right-hand
+    side, or None without d_tensor."""
+    torch = _torch()
+    n, N = int(A_tensor.shape[0]), int(A_tensor.shape[2])
+    code, tdt = _dtype_code(A_tensor.dtype)
+    if not A_tensor.is_cuda:
+        raise ValueError("construct_block_tridiagonal: A_tensor must be a CUDA tensor")
+    A = _blocks_colmajor(A_tensor, n, N)
+    B = _blocks_colmajor(B_tensor.to(dtype=tdt), n, N - 1)
+    L = _lib.load()
+    nnz = int(L.bss_csr_nnz(N, n))
+    dev = A.device
+    crow = torch.empty(N * n + 1, dtype=torch.int32, device=dev)
+    col = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
+    val = torch.empty(max(nnz, 1), dtype=tdt, device=dev)
+    bptr = B.data_ptr() if N > 1 else 0
+    _lib.check(L.bss_csr_assemble(N, n, code, ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(bptr),
+                                  ctypes.c_void_p(crow.data_ptr()), ctypes.c_void_p(col.data_ptr()),
+                                  ctypes.c_void_p(val.data_ptr()), _stream_ptr(stream)))
+    M = torch.sparse_csr_tensor(crow, col[:nnz], val[:nnz], size=(N * n, N * n))
+    d_vec = None
+    if d_tensor is not None:
+        k = int(d_tensor.shape[1])
+        d_vec = d_tensor.permute(2, 0, 1).reshape(N * n, k)
+    return M, d_vec
+
+
+class _SpHandle:
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                _lib.load().bss_spchol_destroy(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+
+class SparseCholeskyData:
+    """The reference's sparse direct-solver comparison
+    (benchmark/benchmark_gpu.jl:75-117) on this GPU: the assembled CSR
+    matrix of construct_block_tridiagonal factored by a general sparse
+    Cholesky (bss_spchol_*; cuSOLVER's GPU csrchol stands in for cuDSS,
+    which this toolkit lacks).  A_tensor, B_tensor, d_tensor as for
+    BlockTriDiagData_batched (no padding); ``csr()`` is a zero-copy sparse
+    CSR view of the assembled matrix after ``analyze_`` or ``factorize_``."""
+
+    def __init__(self, handle: _SpHandle, torch_dtype):
+        torch = _torch()
+        L = _lib.load()
+        self._h = handle
+        N, n, k = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _lib.check(L.bss_spchol_get_dims(handle.ptr, ctypes.byref(N), ctypes.byref(n), ctypes.byref(k)))
+        A, B, d = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        _lib.check(L.bss_spchol_get_tensors(handle.ptr, ctypes.byref(A), ctypes.byref(B), ctypes.byref(d)))
+        self.N, self.n, self.k, self.dtype = N.value, n.value, k.value, torch_dtype
+        es = 8 if torch_dtype == torch.float64 else 4
+        self._ts = "<f8" if es == 8 else "<f4"
+        self._es = es
+        nn = self.n * self.n
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self._dev = dev
+        self.A_tensor = torch.as_tensor(
+            _DevView(A.value, (self.n, self.n, self.N), (es, es * self.n, es * nn), self._ts, handle), device=dev)
+        self.B_tensor = torch.as_tensor(
+            _DevView(B.value, (self.n, self.n, max(self.N - 1, 0)), (es, es * self.n, es * nn), self._ts, handle),
+            device=dev)
+        self.d_tensor = torch.as_tensor(
+            _DevView(d.value, (self.n, self.k, self.N), (es, es * self.n, es * self.n * self.k), self._ts, handle),
+            device=dev)
+
+    @property
+    def handle(self):
+        return self._h.ptr
+
+    def csr(self):
+        torch = _torch()
+        rp, ci, v, nnz = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_int64()
+        _lib.check(_lib.load().bss_spchol_get_csr(self.handle, ctypes.byref(rp), ctypes.byref(ci), ctypes.byref(v),
+                                                  ctypes.byref(nnz)))
+        rows = self.N * self.n
+        crow = torch.as_tensor(_DevView(rp.value, (rows + 1,), (4,), "<i4", self._h), device=self._dev)
+        col = torch.as_tensor(_DevView(ci.value, (nnz.value,), (4,), "<i4", self._h), device=self._dev)
+        val = torch.as_tensor(_DevView(v.value, (nnz.value,), (self._es,), self._ts, self._h), device=self._dev)
+        return torch.sparse_csr_tensor(crow, col, val, size=(rows, rows))
+
+
+def initialize_sparse_cholesky(N: int, n: int, T=None, *, k: int = 1, stream=None) -> SparseCholeskyData:
+    """Sparse direct-solver comparison (benchmark/benchmark_gpu.jl:75-117):
+    same tensors as initialize_batched; analyze_/factorize_/solve_ run the
+    analysis, factorization and solve phases on the assembled CSR matrix."""
+    torch = _torch()
+    code, tdt = _dtype_code(torch.float64 if T is None else T)
+    h = ctypes.c_void_p()
+    torch.cuda.current_device()
+    _lib.check(_lib.load().bss_spchol_create(int(N), int(n), int(k), code, _stream_ptr(stream), ctypes.byref(h)))
+    return SparseCholeskyData(_SpHandle(h.value), tdt)
+
+
+def analyze_(data: SparseCholeskyData) -> None:
+    """The analysis phase of the sparse comparison (cudss("analysis", ...),
+    benchmark/benchmark_gpu.jl:93): assemble the CSR matrix from A_tensor /
+    B_tensor and run the symbolic factorization."""
+    _lib.check(_lib.load().bss_spchol_analyze(data.handle))
+
+
 class _CpuHandle:
     def __init__(self, ptr):
         self.ptr = ptr
@@ -304,6 +433,9 @@ def factorize_(data, check: bool = False) -> None:
     if isinstance(data, ReferenceAlgorithmData):
         _lib.check(_lib.load().bss_refalgo_factorize(data.handle))
         return
+    if isinstance(data, SparseCholeskyData):
+        _lib.check(_lib.load().bss_spchol_factorize(data.handle))
+        return
     _lib.check(_lib.load().bss_factorize(data.handle))
     if check:
         synchronize(data)
@@ -317,6 +449,9 @@ def solve_(data, check: bool = False) -> None:
         return
     if isinstance(data, ReferenceAlgorithmData):
         _lib.check(_lib.load().bss_refalgo_solve(data.handle))
+        return
+    if isinstance(data, SparseCholeskyData):
+        _lib.check(_lib.load().bss_spchol_solve(data.handle))
         return
     _lib.check(_lib.load().bss_solve(data.handle))
     if check:

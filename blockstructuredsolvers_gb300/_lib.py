@@ -46,6 +46,8 @@ EXPORTS = (
     "bss_cpu_failed_block", "bss_tc_selftest", "bss_diag_wide_occupancy",
     "bss_refalgo_create", "bss_refalgo_destroy", "bss_refalgo_get_tensors", "bss_refalgo_get_dims",
     "bss_refalgo_factorize", "bss_refalgo_solve",
+    "bss_csr_nnz", "bss_csr_assemble", "bss_spchol_create", "bss_spchol_destroy", "bss_spchol_get_tensors",
+    "bss_spchol_get_csr", "bss_spchol_get_dims", "bss_spchol_analyze", "bss_spchol_factorize", "bss_spchol_solve",
 )
 
 
@@ -218,9 +220,21 @@ def load(path: str | None = None):
     L.bss_refalgo_get_dims.argtypes = [vp, ctypes.POINTER(i64), ctypes.POINTER(i64), ctypes.POINTER(i64)]
     L.bss_refalgo_factorize.argtypes = [vp]
     L.bss_refalgo_solve.argtypes = [vp]
+    L.bss_csr_nnz.argtypes = [i64, i64]
+    L.bss_csr_nnz.restype = i64
+    L.bss_csr_assemble.argtypes = [i64, i64, i32, vp, vp, vp, vp, vp, vp]
+    L.bss_spchol_create.argtypes = [i64, i64, i64, i32, vp, ctypes.POINTER(vp)]
+    L.bss_spchol_destroy.argtypes = [vp]
+    L.bss_spchol_get_tensors.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    L.bss_spchol_get_csr.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                     ctypes.POINTER(i64)]
+    L.bss_spchol_get_dims.argtypes = [vp, ctypes.POINTER(i64), ctypes.POINTER(i64), ctypes.POINTER(i64)]
+    L.bss_spchol_analyze.argtypes = [vp]
+    L.bss_spchol_factorize.argtypes = [vp]
+    L.bss_spchol_solve.argtypes = [vp]
     for name in EXPORTS:
         if name not in ("bss_default_options", "bss_last_error_string", "bss_version", "bss_kernel_launches",
-                        "bss_server_default_options", "bss_autotune_clear"):
+                        "bss_server_default_options", "bss_autotune_clear", "bss_csr_nnz"):
             getattr(L, name).restype = ctypes.c_int
     if path is None:
         _lib = L

@@ -363,6 +363,41 @@ int bss_refalgo_get_dims(bss_refalgo *h, int64_t *N, int64_t *n, int64_t *k);
 int bss_refalgo_factorize(bss_refalgo *h);
 int bss_refalgo_solve(bss_refalgo *h);
 
+/* ---- sparse assembly and a general sparse Cholesky (comparison) ------------
+ * bss_csr_assemble replaces construct_block_tridiagonal
+ * (benchmark/utils.jl:59-103): from N column-major n x n blocks A (device)
+ * and N-1 blocks B it writes the (N n) x (N n) matrix with A_i on the
+ * diagonal, B_i at block (i, i+1) and B_i^T at block (i+1, i) as CSR --
+ * 0-based int32 row_ptr (N n + 1) and col_idx (nnz), column indices ascending
+ * in every row, every entry of every block stored (explicit zeros kept, as
+ * the reference's sparse(I, J, V) keeps them), values copied bit for bit.
+ * nnz = bss_csr_nnz(N, n) = n^2 (3N - 2) must be below 2^31.  Asynchronous
+ * on `stream`.
+ *
+ * bss_spchol_* replaces the reference's sparse direct-solver comparison
+ * (benchmark/benchmark_gpu.jl:75-117: analysis, factorization, solve of the
+ * assembled SPD matrix with cuDSS).  cuDSS is not in this toolkit; the
+ * phases run on cuSOLVER's GPU sparse Cholesky (csrcholAnalysis,
+ * csrcholFactor, csrcholSolve) over the bss_csr_assemble matrix.  Tensors
+ * as for bss_create_batched without padding (A n x n x N, B n x n x (N-1),
+ * d n x k x N, column-major, device); analyze assembles the CSR matrix and
+ * runs the symbolic phase; factorize re-assembles the values (analyzing
+ * first if needed) and factors, returning BSS_ERR_NOT_SPD on a zero pivot;
+ * solve overwrites d with the solution.  The library phases synchronise the
+ * stream. */
+int64_t bss_csr_nnz(int64_t N, int64_t n);
+int bss_csr_assemble(int64_t N, int64_t n, int32_t dtype, const void *A, const void *B, int32_t *row_ptr,
+                     int32_t *col_idx, void *vals, void *stream);
+typedef struct bss_spchol bss_spchol;
+int bss_spchol_create(int64_t N, int64_t n, int64_t k, int32_t dtype, void *stream, bss_spchol **out);
+int bss_spchol_destroy(bss_spchol *h);
+int bss_spchol_get_tensors(bss_spchol *h, void **A, void **B, void **d);
+int bss_spchol_get_csr(bss_spchol *h, int32_t **row_ptr, int32_t **col_idx, void **vals, int64_t *nnz);
+int bss_spchol_get_dims(bss_spchol *h, int64_t *N, int64_t *n, int64_t *k);
+int bss_spchol_analyze(bss_spchol *h);
+int bss_spchol_factorize(bss_spchol *h);
+int bss_spchol_solve(bss_spchol *h);
+
 /* Diagnostic (no counterpart in the reference): one tensor-core product
  * C = X^T Y of n x n FP32 blocks (n <= 128) through the wide kernel's
  * tcgen05 3xTF32 path, compared with an FP64 product of the same inputs;

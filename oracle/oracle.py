@@ -417,6 +417,51 @@ def assemble_dense(A: np.ndarray, B: np.ndarray) -> np.ndarray:
     return M
 
 
+def construct_block_tridiagonal(A: np.ndarray, B: np.ndarray, d: np.ndarray | None = None):
+    """benchmark/utils.jl:59-103: the (N n) x (N n) matrix as coordinate
+    triples (I, J, V), pushed for every entry of every stored block in the
+    reference's loop order (block row i, block column j in {i-1, i, i+1}
+    with A_i, B_i or B_{j}^T, then row, then column), turned into compressed
+    rows: returns ``(row_ptr, col_idx, vals, d_vec)`` with 0-based int32
+    indices, columns ascending within a row, explicit zeros kept (as
+    Julia's ``sparse(I, J, V)`` keeps them), d_vec = vcat(d_list...) of shape
+    (N n, k) or None.  Bit-exact: the values are copies of the block entries.
+    """
+    A = np.asarray(A)
+    N, n, _ = A.shape
+    I_parts, J_parts, V_parts = [], [], []
+    rr, cc = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    for i in range(N):                       # utils.jl:72
+        for j in (i - 1, i, i + 1):          # utils.jl:74-86 (other blocks skipped)
+            if j < 0 or j >= N:
+                continue
+            if j == i:
+                blk = A[i]
+            elif j == i + 1:
+                blk = B[i]
+            else:
+                blk = B[j].T
+            I_parts.append((i * n + rr).ravel())   # utils.jl:89-94: row-major pushes
+            J_parts.append((j * n + cc).ravel())
+            V_parts.append(np.asarray(blk).ravel())
+    I = np.concatenate(I_parts)
+    J = np.concatenate(J_parts)
+    V = np.concatenate(V_parts)
+    order = np.lexsort((J, I))               # compressed rows, columns ascending
+    I, J, V = I[order], J[order], V[order]
+    if I.size > 1:
+        dup = (I[1:] == I[:-1]) & (J[1:] == J[:-1])
+        assert not dup.any(), "block pattern has no duplicate coordinates"
+    row_ptr = np.zeros(N * n + 1, dtype=np.int64)
+    np.add.at(row_ptr, I + 1, 1)
+    row_ptr = np.cumsum(row_ptr).astype(np.int32)
+    d_vec = None
+    if d is not None:
+        d = np.asarray(d)
+        d_vec = d.reshape(N * n, d.shape[2])  # utils.jl:100: vcat(d_list...)
+    return row_ptr, J.astype(np.int32), V, d_vec
+
+
 def dense_solve(A, B, d) -> np.ndarray:
     N, n, _ = A.shape
     k = d.shape[2]

@@ -173,3 +173,34 @@ def test_summary_json_consistent():
     for N, ent in js["planner"].items():
         levels, coarse = O.reference_plan(int(N))
         assert [list(l) for l in levels] == ent["levels"] and coarse == ent["coarsest"]
+
+
+@pytest.mark.parametrize("N,n,k", [(1, 4, 1), (2, 3, 2), (7, 5, 1), (12, 8, 3), (5, 33, 1)])
+def test_sparse_assembly_restatement(N, n, k):
+    """construct_block_tridiagonal (benchmark/utils.jl:59-103) restated:
+    the CSR matrix equals the dense assembly entry for entry, every block
+    entry is stored (nnz = n^2 (3N - 2), explicit zeros kept), rows are
+    sorted, d_vec = vcat(d_list...), and scipy's own COO -> CSR conversion
+    of the same triples gives the same arrays."""
+    rng = np.random.default_rng(N * 100 + n)
+    A = rng.standard_normal((N, n, n))
+    B = rng.standard_normal((max(N - 1, 0), n, n))
+    if N > 1:
+        B[0, 0, :] = 0.0  # explicit zeros stay stored
+    d = rng.standard_normal((N, n, k))
+    rp, ci, v, dv = O.construct_block_tridiagonal(A, B, d)
+    assert rp.dtype == np.int32 and ci.dtype == np.int32
+    assert rp[-1] == n * n * (3 * N - 2) == ci.size == v.size
+    M = O.assemble_dense(A, B)
+    dense = np.zeros_like(M)
+    for R in range(N * n):
+        cols = ci[rp[R]:rp[R + 1]]
+        assert np.all(np.diff(cols) > 0)
+        dense[R, cols] = v[rp[R]:rp[R + 1]]
+    assert np.array_equal(dense, M)
+    assert np.array_equal(dv, np.concatenate([d[i] for i in range(N)], axis=0))
+    sp = pytest.importorskip("scipy.sparse")
+    rows = np.repeat(np.arange(N * n), np.diff(rp))
+    C = sp.coo_matrix((v, (rows, ci)), shape=M.shape).tocsr()
+    C.sort_indices()
+    assert np.array_equal(C.indptr, rp) and np.array_equal(C.indices, ci) and np.array_equal(C.data, v)
