@@ -736,11 +736,11 @@ int residual_check(bss_handle *h)
     h->need_anorm = false;
     if (wn) BSS_CUDA(cudaMemsetAsync(&st->need_anorm, 0, sizeof(int), h->ls));
     if (h->levels[0].t == F32)
-        BSS_CUDA((launch_residual<double, float>((const double *)h->A, (const double *)h->B, h->x64, d64,
-                                                 (float *)h->c0, h->N, (int)h->n, (int)h->k, wn, st, h->ls)));
+        BSS_CUDA((launch_residual_df<float>((const double *)h->A, (const double *)h->B, h->x64, d64,
+                                            (float *)h->c0, h->N, (int)h->n, (int)h->k, wn, st, h->ls)));
     else
-        BSS_CUDA((launch_residual<double, double>((const double *)h->A, (const double *)h->B, h->x64, d64,
-                                                  (double *)h->c0, h->N, (int)h->n, (int)h->k, wn, st, h->ls)));
+        BSS_CUDA((launch_residual_df<double>((const double *)h->A, (const double *)h->B, h->x64, d64,
+                                             (double *)h->c0, h->N, (int)h->n, (int)h->k, wn, st, h->ls)));
     BSS_CUDA(launch_relres(st, h->opt.tol, h->ls));
     BSS_CUDA(cudaMemcpyAsync(h->h_st, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->ls));
     return BSS_OK;
@@ -871,11 +871,11 @@ int capture_mixed_solve(bss_handle *h)
     BSS_CUDA(cudaStreamBeginCaptureToGraph(h->cap_stream2, wbody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     BSS_CUDA(cudaMemsetAsync(&st->rnorm, 0, 2 * sizeof(unsigned long long), h->ls));
     if (c_is_f32)
-        BSS_CUDA((launch_residual<double, float>((const double *)h->A, (const double *)h->B, h->x64, d64,
-                                                 (float *)h->c0, h->N, (int)h->n, (int)h->k, -1, st, h->ls)));
+        BSS_CUDA((launch_residual_df<float>((const double *)h->A, (const double *)h->B, h->x64, d64,
+                                            (float *)h->c0, h->N, (int)h->n, (int)h->k, -1, st, h->ls)));
     else
-        BSS_CUDA((launch_residual<double, double>((const double *)h->A, (const double *)h->B, h->x64, d64,
-                                                  (double *)h->c0, h->N, (int)h->n, (int)h->k, -1, st, h->ls)));
+        BSS_CUDA((launch_residual_df<double>((const double *)h->A, (const double *)h->B, h->x64, d64,
+                                             (double *)h->c0, h->N, (int)h->n, (int)h->k, -1, st, h->ls)));
     BSS_CUDA(launch_relres_control(st, h->opt.tol, h->opt.max_refine, hloop, hcorr, h->ls));
     const long long k2 = launch_count();
     cudaGraph_t g2 = nullptr;

@@ -117,3 +117,26 @@ extern "C" int bss_diag_wide_occupancy(int64_t *out)
     out[5] = (int64_t)smem;
     return BSS_OK;
 }
+
+// Diagnostic: the residual r = d - T x of an FP64 system by the exact FP64
+// kernel (method 0) or by the refinement's double-float kernel (method 1),
+// written to r (device, n x k per block); synchronises.
+extern "C" int bss_diag_residual(int64_t N, int64_t n, int64_t k, int32_t method, const double *A, const double *B,
+                                 const double *x, const double *d, double *r, void *stream)
+{
+    if (N < 1 || n < 1 || k < 1 || !A || (N > 1 && !B) || !x || !d || !r || (method != 0 && method != 1))
+        return fail(BSS_ERR_ARG, "bss_diag_residual: bad argument");
+    if (residual_smem_bytes<double>((int)n, 1) > (size_t)200 * 1024)
+        return fail(BSS_ERR_ARG, "bss_diag_residual: block size too large for the residual kernel");
+    cudaStream_t s = (cudaStream_t)stream;
+    DevStatus *st = nullptr;
+    BSS_CUDA(cudaMallocAsync((void **)&st, sizeof(DevStatus), s));
+    BSS_CUDA(cudaMemsetAsync(st, 0, sizeof(DevStatus), s));
+    cudaError_t e = method == 0
+                        ? launch_residual<double, double>(A, B, x, d, r, N, (int)n, (int)k, 1, st, s)
+                        : launch_residual_df<double>(A, B, x, d, r, N, (int)n, (int)k, 1, st, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(st, s);
+    if (e != cudaSuccess) return cuda_fail(e, "bss_diag_residual");
+    return BSS_OK;
+}

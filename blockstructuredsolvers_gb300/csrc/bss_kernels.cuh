@@ -1932,6 +1932,297 @@ __global__ void __launch_bounds__(RES_THREADS, 3) residual_kernel(const T *__res
     residual_body<T, Tr>(A, B, x, d, r, N, n, ktot, j0, k, b0, b0 + per_cta, with_norm, st);
 }
 
+// ---------------------------------------------------------------------------
+// Refinement residual on the FP32 pipe ("double-float"): r = d - T x for FP64
+// A, B, x, d without FP64 instructions in the inner loops.  On GB300 the FP64
+// pipe retires ~2 FMA/clk/SM, which bounds the FP64 residual at 3 n^2 FMAs per
+// block (0.32 ms at N = 16384, n = 64) against 0.16 ms to stream A and B from
+// HBM; here every product runs on the 128-lane FP32 pipe.
+//
+// Representation: an FP64 value a becomes (a_hi, a_lo), a_hi = a truncated to
+// 24 significant bits and a_lo = the next 23 bits, both exact FP32 values, so
+// |a - a_hi - a_lo| < 2^-46 |a| (split with integer operations only; values
+// below 2^-126 in magnitude become 0).  A product a x is a_hi x_hi, made
+// exact with an FMA (TwoProd: p + e), plus a_hi x_lo + a_lo x_hi (each within
+// 2^-48 |a x|); a_lo x_lo (< 2^-46 |a x|) is dropped.  Sums keep the high
+// parts exact with TwoSum and gather every lower-order term in an FP32 low
+// word.  The computed r differs from d - T x by less than about
+// 2^-45 (|d| + |T| |x|) per entry -- far below the refinement's normwise
+// target (1e-12) -- and the r handed to the FP32 correction is rounded to
+// FP32 anyway.  The p and TwoSum operations use the _rn intrinsics so that
+// no FMA contraction can change them.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 split_df(double a)
+{
+    const unsigned hi = (unsigned)__double2hiint(a), lo = (unsigned)__double2loint(a);
+    const unsigned mag = hi & 0x7FFFFFFFu;
+    // exponent rebiased 1023 -> 127, then the top 23 mantissa bits (20 from
+    // the high word, 3 from the low word) shifted in; sign restored
+    const unsigned hb0 = __funnelshift_l(lo, mag - 0x38000000u, 3) | (hi & 0x80000000u);
+    const unsigned hb = mag < 0x38100000u ? 0u : hb0;  // |a| < 2^-126: 0
+    // the next 23 bits (low word bits 6 .. 28) as an integer q < 2^23:
+    // float(2^23 + q) - 2^23 is exact, scaled by 2^-46 in the same FMA, then
+    // by the signed power of two of a_hi (its sign and exponent bits)
+    const float q = fmaf(__uint_as_float(((lo >> 6) & 0x7FFFFFu) | 0x4B000000u), 0x1p-46f, -0x1p-23f);
+    return make_float2(__uint_as_float(hb), q * __uint_as_float(hb & 0xFF800000u));
+}
+
+// (sh, sl) += (ah + al) (xh + xl)
+__device__ __forceinline__ void df_mac(float ah, float al, float xh, float xl, float &sh, float &sl)
+{
+    const float p = __fmul_rn(ah, xh);
+    const float e = fmaf(ah, xh, -p);
+    const float s = __fadd_rn(sh, p);
+    const float bb = __fsub_rn(s, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    sh = s;
+    sl += (e + err) + fmaf(ah, xl, al * xh);
+}
+
+// (sh, sl) += (bh, bl)
+__device__ __forceinline__ void df_add(float bh, float bl, float &sh, float &sl)
+{
+    const float s = __fadd_rn(sh, bh);
+    const float bb = __fsub_rn(s, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+    sh = s;
+    sl += err + bl;
+}
+
+// one pass of RHS columns jb .. jb+KB-1 over this thread's column range:
+// t = A_i(row, c0:c1) x_i + B_i(row, c0:c1) x_{i+1}; B_i staged (split) for
+// the transposed product; the |A| + |B| row-sum partial when asked
+template <int KB, bool NORM>
+__device__ __forceinline__ void residual_rows_df(const double *__restrict__ Ag, const double *__restrict__ Bg,
+                                                 bool has_b, int c0, int c1, int n, int LDp, const float2 *x0,
+                                                 const float2 *x1, float2 *sB, bool stage_b, float2 *out, int stride,
+                                                 float *rowsum)
+{
+    float sh[KB], sl[KB];
+#pragma unroll
+    for (int q = 0; q < KB; ++q) sh[q] = sl[q] = 0.0f;
+    float sa = 0.0f;
+    if (has_b) {
+#pragma unroll 4
+        for (int c = c0; c < c1; ++c) {
+            const float2 a = split_df(Ag[(long long)c * n]);
+            const float2 b = split_df(Bg[(long long)c * n]);
+            if (stage_b) sB[c * LDp] = b;
+            if (NORM) sa += fabsf(a.x) + fabsf(b.x);
+#pragma unroll
+            for (int q = 0; q < KB; ++q) {
+                const float2 u = x0[c + q * n], v = x1[c + q * n];
+                df_mac(a.x, a.y, u.x, u.y, sh[q], sl[q]);
+                df_mac(b.x, b.y, v.x, v.y, sh[q], sl[q]);
+            }
+        }
+    } else {
+#pragma unroll 4
+        for (int c = c0; c < c1; ++c) {
+            const float2 a = split_df(Ag[(long long)c * n]);
+            if (NORM) sa += fabsf(a.x);
+#pragma unroll
+            for (int q = 0; q < KB; ++q) {
+                const float2 u = x0[c + q * n];
+                df_mac(a.x, a.y, u.x, u.y, sh[q], sl[q]);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < KB; ++q) out[q * stride] = make_float2(sh[q], sl[q]);
+    if (NORM) *rowsum = sa;
+}
+
+// Same decomposition as residual_body (thread = (row, column part); B_i
+// staged in shared memory for u_{i+1} = B_i^T x_i; x ring and u ping-pong in
+// shared memory), in double-float: shared arrays hold (hi, lo) float pairs.
+// Shared memory: residual_smem_bytes<double>(n, k).
+template <class Tr>
+__device__ __forceinline__ void residual_body_df(const double *__restrict__ A, const double *__restrict__ B,
+                                                 const double *__restrict__ x, const double *__restrict__ d,
+                                                 Tr *__restrict__ r, long long N, int n, int ktot, int j0, int k,
+                                                 long long b0_, long long b1_, int with_norm, DevStatus *st)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int LDp = n + 1;
+    const int nk = n * k;
+    const long long bstride = (long long)n * ktot, coff = (long long)j0 * n;
+    float2 *sB = reinterpret_cast<float2 *>(smem_raw);
+    float2 *sxr = sB + n * LDp;      // [3][nk]
+    float2 *sub = sxr + 3 * nk;      // [2][nk] u_i ping-pong
+    float2 *red = sub + 2 * nk;      // [2][8][nk]
+    float *rowred = reinterpret_cast<float *>(red + 16 * nk);  // [3][8][n]
+    float *rowu = rowred + 24 * n;   // [n]
+    int parts = RES_THREADS / n;
+    parts = parts < 1 ? 1 : (parts > 8 ? 8 : parts);
+    const int tid = threadIdx.x;
+    const int row = tid % n, part = tid / n;
+    const bool active = part < parts;
+    const int c0 = active ? (part * n) / parts : 0, c1 = active ? ((part + 1) * n) / parts : 0;
+    const long long nn = (long long)n * n;
+    const long long b0 = b0_;
+    const long long b1 = b1_ < N ? b1_ : N;
+    if (b0 >= N) return;
+    if (with_norm < 0) with_norm = st->need_anorm;  // graph mode: decided on the device
+    float rmax = 0.0f, xmax = 0.0f, amax = 0.0f;
+    auto xs = [&](long long blk) { return sxr + (int)((blk - b0 + 3) % 3) * nk; };  // blk in [b0-1, b1]
+
+    // prologue: x_{b0-1}, x_{b0}, x_{b0+1}; u_{b0} = B_{b0-1}^T x_{b0-1}
+    for (int e = tid; e < nk; e += blockDim.x) {
+        xs(b0)[e] = split_df(x[b0 * bstride + coff + e]);
+        if (b0 + 1 < N) xs(b0 + 1)[e] = split_df(x[(b0 + 1) * bstride + coff + e]);
+        sub[e] = make_float2(0.0f, 0.0f);
+    }
+    for (int e = tid; e < n; e += blockDim.x) rowu[e] = 0.0f;
+    if (b0 > 0) {
+        float2 *xm = xs(b0 - 1);
+        for (int e = tid; e < nk; e += blockDim.x) xm[e] = split_df(x[(b0 - 1) * bstride + coff + e]);
+        for (int e = tid; e < (int)nn; e += blockDim.x) {
+            const int c = e / n, rr = e - c * n;
+            sB[rr + c * LDp] = split_df(B[(b0 - 1) * nn + e]);
+        }
+        __syncthreads();
+        for (int o = tid; o < nk; o += blockDim.x) {
+            const int j = o / n, rr = o - j * n;
+            float sh = 0.0f, sl = 0.0f;
+            for (int c = 0; c < n; ++c) {
+                const float2 b = sB[c + rr * LDp], v = xm[c + j * n];
+                df_mac(b.x, b.y, v.x, v.y, sh, sl);
+            }
+            sub[o] = make_float2(sh, sl);
+        }
+        if (with_norm)
+            for (int rr = tid; rr < n; rr += blockDim.x) {
+                float s = 0.0f;
+                for (int c = 0; c < n; ++c) s += fabsf(sB[c + rr * LDp].x);
+                rowu[rr] = s;
+            }
+    }
+    __syncthreads();
+
+    for (long long i = b0; i < b1; ++i) {
+        const int par = (int)((i - b0) & 1);
+        const bool has_b = i + 1 < N;
+        const float2 *x0 = xs(i);
+        const float2 *x1 = xs(i + 1);
+        float2 *su = sub + par * nk;         // u_i
+        float2 *sun = sub + (par ^ 1) * nk;  // u_{i+1}
+        // phase 1: t partials from global A_i, B_i; B_i into shared memory
+        if (active) {
+            const double *Ag = A + i * nn + row;
+            const double *Bg = B + i * nn + row;
+            // right-hand sides in compile-time groups (4, then 1); the first
+            // group also stages B_i and, when asked, the |A| + |B| row sums
+            float *rs = rowred + part * n + row;
+            float2 *o = red + part * k * n + row;
+            int jb = 0;
+            if (k >= 4) {
+                if (with_norm)
+                    residual_rows_df<4, true>(Ag, Bg, has_b, c0, c1, n, LDp, x0, x1, sB + row, true, o, n, rs);
+                else
+                    residual_rows_df<4, false>(Ag, Bg, has_b, c0, c1, n, LDp, x0, x1, sB + row, true, o, n, rs);
+                jb = 4;
+            } else {
+                if (with_norm)
+                    residual_rows_df<1, true>(Ag, Bg, has_b, c0, c1, n, LDp, x0, x1, sB + row, true, o, n, rs);
+                else
+                    residual_rows_df<1, false>(Ag, Bg, has_b, c0, c1, n, LDp, x0, x1, sB + row, true, o, n, rs);
+                jb = 1;
+            }
+            for (; jb + 4 <= k; jb += 4)
+                residual_rows_df<4, false>(Ag, Bg, has_b, c0, c1, n, LDp, x0 + jb * n, x1 + jb * n, sB + row, false,
+                                           o + jb * n, n, rs);
+            for (; jb < k; ++jb)
+                residual_rows_df<1, false>(Ag, Bg, has_b, c0, c1, n, LDp, x0 + jb * n, x1 + jb * n, sB + row, false,
+                                           o + jb * n, n, rs);
+        }
+        __syncthreads();
+        // phase 2: u_{i+1} partials from the staged B_i
+        if (active && has_b) {
+            for (int j = 0; j < k; ++j) {
+                float sh = 0.0f, sl = 0.0f;
+                for (int c = c0; c < c1; ++c) {
+                    const float2 b = sB[c + row * LDp], v = x0[c + j * n];
+                    df_mac(b.x, b.y, v.x, v.y, sh, sl);
+                }
+                red[8 * nk + (part * k + j) * n + row] = make_float2(sh, sl);
+            }
+            if (with_norm) {
+                float sbt = 0.0f;
+                for (int c = c0; c < c1; ++c) sbt += fabsf(sB[c + row * LDp].x);
+                rowred[16 * n + part * n + row] = sbt;
+            }
+        }
+        __syncthreads();
+        // phase 3: r_i = d_i - t - u_i; fetch x_{i+2}
+        for (int o = tid; o < nk; o += blockDim.x) {
+            const int j = o / n, rr = o - j * n;
+            const float2 dd = split_df(d[i * bstride + coff + o]);
+            float rh = dd.x, rl = dd.y;
+            float uh = 0.0f, ul = 0.0f;
+            for (int q = 0; q < parts; ++q) {
+                const float2 t = red[(q * k + j) * n + rr];
+                df_add(-t.x, -t.y, rh, rl);
+            }
+            df_add(-su[o].x, -su[o].y, rh, rl);
+            if (has_b)
+                for (int q = 0; q < parts; ++q) {
+                    const float2 u = red[8 * nk + (q * k + j) * n + rr];
+                    df_add(u.x, u.y, uh, ul);
+                }
+            float res_f;
+            if constexpr (std::is_same<Tr, double>::value) {
+                const double res = (double)rh + (double)rl;
+                if (r) r[i * bstride + coff + o] = res;
+                res_f = (float)res;
+            } else {
+                res_f = rh + rl;
+                if (r) r[i * bstride + coff + o] = (Tr)res_f;
+            }
+            rmax = fmaxf(rmax, fabsf(res_f));
+            xmax = fmaxf(xmax, fabsf(x0[o].x));
+            sun[o] = make_float2(uh, ul);
+        }
+        if (with_norm)
+            for (int rr = tid; rr < n; rr += blockDim.x) {
+                float s = rowu[rr], s2 = 0.0f;
+                for (int q = 0; q < parts; ++q) {
+                    s += rowred[q * n + rr];
+                    if (has_b) s2 += rowred[16 * n + q * n + rr];
+                }
+                amax = fmaxf(amax, s);
+                rowu[rr] = has_b ? s2 : 0.0f;
+            }
+        if (i + 2 < N && i + 1 < b1) {
+            float2 *x2 = xs(i + 2);
+            for (int e = tid; e < nk; e += blockDim.x) x2[e] = split_df(x[(i + 2) * bstride + coff + e]);
+        }
+        __syncthreads();
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+        xmax = fmaxf(xmax, __shfl_xor_sync(0xffffffffu, xmax, o));
+        amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomic_max_nonneg(&st->rnorm, (double)rmax);
+        atomic_max_nonneg(&st->xnorm, (double)xmax);
+        if (with_norm) atomic_max_nonneg(&st->anorm, (double)amax);
+    }
+}
+
+template <class Tr>
+__global__ void __launch_bounds__(RES_THREADS, 3) residual_df_kernel(const double *__restrict__ A,
+                                                                  const double *__restrict__ B,
+                                                                  const double *__restrict__ x,
+                                                                  const double *__restrict__ d, Tr *__restrict__ r,
+                                                                  long long N, int n, int ktot, int j0, int k,
+                                                                  long long per_cta, int with_norm, DevStatus *st)
+{
+    const long long b0 = (long long)blockIdx.x * per_cta;
+    residual_body_df<Tr>(A, B, x, d, r, N, n, ktot, j0, k, b0, b0 + per_cta, with_norm, st);
+}
+
 // many systems: one CTA per (system, block range) item
 template <class Tr>
 struct ResidualDesc {
@@ -1952,7 +2243,7 @@ __global__ void __launch_bounds__(RES_THREADS, 3) residual_batch_kernel(const Re
     const WorkItem w = items[blockIdx.x];
     const ResidualDesc<Tr> g = descs[w.desc];
     const long long b0 = (long long)w.p * g.per_cta;
-    residual_body<double, Tr>(g.A, g.B, g.x, g.d, g.r, g.N, g.n, g.k, g.j0, g.kc, b0, b0 + g.per_cta, g.norm, g.st);
+    residual_body_df<Tr>(g.A, g.B, g.x, g.d, g.r, g.N, g.n, g.k, g.j0, g.kc, b0, b0 + g.per_cta, g.norm, g.st);
 }
 
 // one refinement decision on the device (graph mode): relative residual,

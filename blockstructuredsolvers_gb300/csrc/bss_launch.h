@@ -42,6 +42,11 @@ cudaError_t launch_absmax(const T *v, long long count, unsigned long long *dst, 
 template <class T, class Tr>
 cudaError_t launch_residual(const T *A, const T *B, const T *x, const T *d, Tr *r, long long N, int n, int k,
                             int with_norm, DevStatus *st, cudaStream_t s);
+// the refinement residual of FP64 systems in double-float on the FP32 pipe
+// (residual_df_kernel); same arguments as launch_residual<double, Tr>
+template <class Tr>
+cudaError_t launch_residual_df(const double *A, const double *B, const double *x, const double *d, Tr *r,
+                               long long N, int n, int k, int with_norm, DevStatus *st, cudaStream_t s);
 cudaError_t launch_relres(DevStatus *st, double tol, cudaStream_t s);
 cudaError_t launch_relres_control(DevStatus *st, double tol, int max_refine, cudaGraphConditionalHandle hloop,
                                   cudaGraphConditionalHandle hcorr, cudaStream_t s);

@@ -197,6 +197,35 @@ cudaError_t launch_residual(const T *A, const T *B, const T *x, const T *d, Tr *
     return cudaSuccess;
 }
 
+template <class Tr>
+cudaError_t launch_residual_df(const double *A, const double *B, const double *x, const double *d, Tr *r,
+                               long long N, int n, int k, int with_norm, DevStatus *st, cudaStream_t s)
+{
+    auto kern = residual_df_kernel<Tr>;
+    int kc = k;
+    while (kc > 1 && residual_smem_bytes<double>(n, kc) > (size_t)200 * 1024) kc = (kc + 1) / 2;
+    const size_t smem = residual_smem_bytes<double>(n, kc);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int per_sm = ctas_per_sm(kern, RES_THREADS, smem);
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long grid = (long long)sms * (per_sm > 0 ? per_sm : 1);
+    if (grid > N) grid = N;
+    const long long per_cta = (N + grid - 1) / grid;
+    grid = (N + per_cta - 1) / per_cta;
+    for (int j0 = 0; j0 < k; j0 += kc) {
+        const int kk = (k - j0 < kc) ? k - j0 : kc;
+        kern<<<(unsigned)grid, RES_THREADS, smem, s>>>(A, B, x, d, r, N, n, k, j0, kk, per_cta,
+                                                       (with_norm && j0 == 0) ? with_norm : 0, st);
+        count_launch();
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 template <class Tc>
 cudaError_t launch_update(double *x, const Tc *c, long long count, int assign, cudaStream_t s)
 {

@@ -15,6 +15,10 @@ template cudaError_t launch_assemble_schur<double, float, double>(const double *
 template cudaError_t launch_residual<double, float>(const double *, const double *, const double *,
                                                     const double *, float *, long long, int, int, int, DevStatus *,
                                                     cudaStream_t);
+template cudaError_t launch_residual_df<float>(const double *, const double *, const double *, const double *,
+                                               float *, long long, int, int, int, DevStatus *, cudaStream_t);
+template cudaError_t launch_residual_df<double>(const double *, const double *, const double *, const double *,
+                                                double *, long long, int, int, int, DevStatus *, cudaStream_t);
 template cudaError_t launch_convert<double, float>(float *, const double *, long long, cudaStream_t);
 template cudaError_t launch_convert<double, double>(double *, const double *, long long, cudaStream_t);
 template cudaError_t launch_convert<float, float>(float *, const float *, long long, cudaStream_t);

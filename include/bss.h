@@ -410,6 +410,14 @@ int bss_tc_selftest(int64_t n, double *max_rel_err);
  * thread, dynamic shared memory bytes. */
 int bss_diag_wide_occupancy(int64_t *out);
 
+/* Diagnostic (no counterpart in the reference): r = d - T x of an FP64
+ * system (A, B, x, d, r device, column-major n x n / n x k blocks) by the
+ * exact FP64 residual kernel (method 0) or by the double-float kernel on
+ * the FP32 pipe that the mixed-precision refinement uses (method 1).
+ * Synchronises `stream`. */
+int bss_diag_residual(int64_t N, int64_t n, int64_t k, int32_t method, const double *A, const double *B,
+                      const double *x, const double *d, double *r, void *stream);
+
 /* Number of CUDA kernels this library has launched in this process, over
  * all handles (no counterpart in the reference; benchmarks report it). */
 int64_t bss_kernel_launches(void);

@@ -204,3 +204,35 @@ def test_sparse_assembly_restatement(N, n, k):
     C = sp.coo_matrix((v, (rows, ci)), shape=M.shape).tocsr()
     C.sort_indices()
     assert np.array_equal(C.indptr, rp) and np.array_equal(C.indices, ci) and np.array_equal(C.data, v)
+
+
+def _split_df_restated(a):
+    """The double-float split of the refinement residual kernel restated on
+    the bit patterns: a_hi = a truncated to 24 significant bits (exponent
+    rebiased, top 23 mantissa bits), a_lo = the next 23 bits scaled by
+    a_hi's signed power of two; |a| < 2^-126 -> (0, 0)."""
+    b = np.ascontiguousarray(a, np.float64).view(np.uint64)
+    hi = (b >> np.uint64(32)).astype(np.uint64)
+    lo = (b & np.uint64(0xFFFFFFFF)).astype(np.uint64)
+    mag = hi & np.uint64(0x7FFFFFFF)
+    t = (mag - np.uint64(0x38000000)) & np.uint64(0xFFFFFFFF)
+    hb0 = (((t << np.uint64(3)) | (lo >> np.uint64(29))) & np.uint64(0xFFFFFFFF)) | (hi & np.uint64(0x80000000))
+    hb = np.where(mag < np.uint64(0x38100000), np.uint64(0), hb0).astype(np.uint32)
+    magic = (((lo >> np.uint64(6)) & np.uint64(0x7FFFFF)) | np.uint64(0x4B000000)).astype(np.uint32)
+    q = (magic.view(np.float32).astype(np.float64) * 2.0 ** -46 - 2.0 ** -23).astype(np.float32)
+    assert np.all(q.astype(np.float64) == magic.view(np.float32).astype(np.float64) * 2.0 ** -46 - 2.0 ** -23)
+    hbe = (hb & np.uint32(0xFF800000)).view(np.float32)
+    return hb.view(np.float32), (q * hbe).astype(np.float32)
+
+
+def test_double_float_split_bits():
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal(20000) * 2.0 ** rng.integers(-90, 91, size=20000)
+    a = np.concatenate([a, [0.0, -0.0, 1.0, -1.0, 2.0 ** -126, 3.0 * 2.0 ** -120, np.nextafter(1.0, 2.0)]])
+    h, l = _split_df_restated(a)
+    err = np.abs(a - h.astype(np.float64) - l.astype(np.float64))
+    big = np.abs(a) >= 2.0 ** -100
+    assert np.all(err[big] < 2.0 ** -46 * np.abs(a[big]))
+    assert np.all(np.abs(h.astype(np.float64)) <= np.abs(a))      # truncation toward zero
+    assert np.all(np.sign(h[a != 0]) == np.sign(a[a != 0]))
+    assert h[-7] == 0.0 and l[-7] == 0.0 and h[-6] == 0.0
