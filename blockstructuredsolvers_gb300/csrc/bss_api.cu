@@ -209,10 +209,9 @@ int bss::plan_handle(bss_handle *h)
             long long target = h->opt.target_partitions > 0
                                    ? h->opt.target_partitions
                                    : (tuned ? std::max(1LL, wave * te.wave_mult_x4 / 4) : wave);
-            // mixed: the coarsest level is FP64, whose per-SM rate is ~1/64 of FP32,
-            // so halve down to 2 blocks; plain: 4 balances levels against chain length
-            long long cutoff = h->opt.seq_cutoff > 0 ? h->opt.seq_cutoff
-                                                     : (tuned ? te.seq_cutoff : (mixed ? 2 : 4));
+            // a coarsest chain of 4 blocks balances one more level against a
+            // longer sequential chain
+            long long cutoff = h->opt.seq_cutoff > 0 ? h->opt.seq_cutoff : (tuned ? te.seq_cutoff : 4);
             plan_auto(h->N, target, cutoff, Ns, Qs, coarsest);
         }
     }
@@ -227,12 +226,15 @@ int bss::plan_handle(bss_handle *h)
         h->levels.push_back(L);
     }
     {
+        // the sequential coarsest level: plain in the tensor dtype; mixed in
+        // FP32 like every other level (the FP64 refinement corrects the whole
+        // factorization, and GB300's FP64 pipe runs at ~1/64 of FP32)
         Level L;
         L.N = coarsest;
         L.Q = 0;
         L.seq = true;
-        L.t = D;  // plain: the tensor dtype; mixed: FP64 coarsest Cholesky
-        L.tin = D;
+        L.t = mixed ? F32 : D;
+        L.tin = h->levels.empty() ? D : L.t;
         h->levels.push_back(L);
     }
     const int nlev = (int)h->levels.size();

@@ -554,6 +554,7 @@ int build_batch(bss_batch *b)
         plan_asm_schur<float, float, double>(B, l);
     }
     plan_factor_level<double, double>(B, 0, true);
+    plan_factor_level<double, float>(B, 0, true);  // mixed systems short enough to have no partitioned level
     plan_factor_level<float, float>(B, 0, true);
     if (!b->mixed) {
         plan_chain_solve(B, maxpart, B.solve);
