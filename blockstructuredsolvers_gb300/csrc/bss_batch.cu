@@ -486,9 +486,17 @@ void plan_vec(Builder &B, int op, std::vector<std::function<Step(char *)>> &dst)
     });
 }
 
+// residual CTA shape per block-size class: 512 threads for the wide class
+// (one CTA per SM fits its staged B_i), 256 otherwise
+inline size_t res_smem(int nb, int n, int k)
+{
+    return nb == (int)WIDE_CLASS ? residual_df_smem_bytes<512>(n, k) : residual_df_smem_bytes<256>(n, k);
+}
+
 template <class Tr>
 void plan_resid(Builder &B, int nb, std::vector<std::function<Step(char *)>> &dst)
 {
+    const bool wide = nb == (int)WIDE_CLASS;
     bss_batch *b = B.b;
     std::vector<ResidualDesc<Tr>> descs;
     std::vector<WorkItem> items;
@@ -498,14 +506,14 @@ void plan_resid(Builder &B, int nb, std::vector<std::function<Step(char *)>> &ds
         if ((h->levels[0].t == F64) != std::is_same<Tr, double>::value || nb_class(h->n) != nb) continue;
         const long long per = std::max(1LL, std::min(h->N, 32LL));
         int kc = (int)h->k;  // column chunk whose shared memory fits
-        while (kc > 1 && residual_smem_bytes<double>((int)h->n, kc) > (size_t)200 * 1024) kc = (kc + 1) / 2;
+        while (kc > 1 && res_smem(nb, (int)h->n, kc) > SMEM_CTA_MAX) kc = (kc + 1) / 2;
         for (int j0 = 0; j0 < h->k; j0 += kc) {
             const int kk = (int)std::min<long long>(kc, h->k - j0);
             ResidualDesc<Tr> d{(const double *)h->A, (const double *)h->B, h->x64, (const double *)h->d,
                                (Tr *)h->c0, h->N, (int)h->n, (int)h->k, j0, kk, j0 == 0 ? -1 : 0, per, h->st};
             const int di = (int)descs.size();
             descs.push_back(d);
-            smem = std::max(smem, residual_smem_bytes<double>((int)h->n, kk));
+            smem = std::max(smem, res_smem(nb, (int)h->n, kk));
             for (long long c = 0; c * per < h->N; ++c) items.push_back(WorkItem{di, (int)c});
         }
     }
@@ -516,12 +524,16 @@ void plan_resid(Builder &B, int nb, std::vector<std::function<Step(char *)>> &ds
         Step st;
         st.what = std::string("plan_resid") + " items=" + std::to_string(ni) + " smem=" + std::to_string(smem);
         st.run = [=](cudaStream_t s) {
-            auto kern = residual_batch_kernel<Tr>;
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-            kern<<<ni, RES_THREADS, smem, s>>>((const ResidualDesc<Tr> *)(base + od), (const WorkItem *)(base + oi));
-            count_launch();
-            return cudaGetLastError();
+            auto run = [&](auto kern, int threads) {
+                cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e != cudaSuccess) return e;
+                e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+                if (e != cudaSuccess) return e;
+                kern<<<ni, threads, smem, s>>>((const ResidualDesc<Tr> *)(base + od), (const WorkItem *)(base + oi));
+                count_launch();
+                return cudaGetLastError();
+            };
+            return wide ? run(residual_batch_kernel<Tr, 512>, 512) : run(residual_batch_kernel<Tr, 256>, 256);
         };
         return st;
     });
@@ -784,14 +796,13 @@ extern "C" int bss_batch_create(int32_t nsys, const int64_t *N, const int64_t *n
             break;
         }
         // The plan of a system depends only on its own N and the chain length,
-        // so its result is the same whichever systems share the batch.  Plain:
-        // systems shorter than two chains run as one sequential chain (the
-        // cheapest schedule; the batch supplies the parallelism).  Mixed: the
-        // coarsest level is FP64, so every system is partitioned down to 2.
+        // so its result is the same whichever systems share the batch.
+        // Systems shorter than two chains run as one sequential chain (the
+        // cheapest schedule; the batch supplies the parallelism).
         const long long chain = batch_chain_blocks(b->opt, (int)n[s], dtype);
         h->opt.plan = BSS_PLAN_AUTO;
         h->opt.target_partitions = (int)std::max<long long>(1, N[s] / chain);
-        if (!b->mixed && N[s] < 2 * chain) h->opt.seq_cutoff = (int)std::max<long long>(1, N[s]);
+        if (N[s] < 2 * chain) h->opt.seq_cutoff = (int)std::max<long long>(1, N[s]);
         rc = plan_handle(h);
         h->arena_bytes = (h->arena_bytes + 255) & ~(size_t)255;
         bytes += h->arena_bytes;

@@ -2033,11 +2033,34 @@ __device__ __forceinline__ void residual_rows_df(const double *__restrict__ Ag, 
     if (NORM) *rowsum = sa;
 }
 
+// column parts per block row for a CTA of THREADS threads (1 .. 8)
+template <int THREADS>
+__host__ __device__ constexpr int res_parts(int n)
+{
+    return THREADS / n < 1 ? 1 : (THREADS / n > 8 ? 8 : THREADS / n);
+}
+
+// largest dynamic shared memory of one CTA on sm_103a
+constexpr size_t SMEM_CTA_MAX = 227 * 1024;
+
+// threads of a double-float residual CTA: 512 for blocks wider than 64 (one
+// CTA per SM fits the staged B_i), else 256
+__host__ __device__ constexpr int res_df_threads(int n) { return n > 64 ? 512 : 256; }
+
+// shared memory of residual_body_df: staged B_i (n (n+1)), x ring (3 nk),
+// u ping-pong (2 nk) and the t / u partials (2 parts nk) as (hi, lo) pairs,
+// plus the FP32 norm partials (25 n)
+template <int THREADS>
+__host__ __device__ constexpr size_t residual_df_smem_bytes(int n, int k)
+{
+    return (size_t)(n * (n + 1) + 5 * n * k + 2 * res_parts<THREADS>(n) * n * k) * 8 + (size_t)25 * n * 4;
+}
+
 // Same decomposition as residual_body (thread = (row, column part); B_i
 // staged in shared memory for u_{i+1} = B_i^T x_i; x ring and u ping-pong in
 // shared memory), in double-float: shared arrays hold (hi, lo) float pairs.
-// Shared memory: residual_smem_bytes<double>(n, k).
-template <class Tr>
+// Shared memory: residual_df_smem_bytes<THREADS>(n, k).
+template <class Tr, int THREADS>
 __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, const double *__restrict__ B,
                                                  const double *__restrict__ x, const double *__restrict__ d,
                                                  Tr *__restrict__ r, long long N, int n, int ktot, int j0, int k,
@@ -2050,11 +2073,11 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
     float2 *sB = reinterpret_cast<float2 *>(smem_raw);
     float2 *sxr = sB + n * LDp;      // [3][nk]
     float2 *sub = sxr + 3 * nk;      // [2][nk] u_i ping-pong
-    float2 *red = sub + 2 * nk;      // [2][8][nk]
-    float *rowred = reinterpret_cast<float *>(red + 16 * nk);  // [3][8][n]
+    const int parts = res_parts<THREADS>(n);
+    float2 *red = sub + 2 * nk;      // [2][parts][nk]
+    float2 *redu = red + parts * nk;  // u partials
+    float *rowred = reinterpret_cast<float *>(red + 2 * parts * nk);  // [3][8][n]
     float *rowu = rowred + 24 * n;   // [n]
-    int parts = RES_THREADS / n;
-    parts = parts < 1 ? 1 : (parts > 8 ? 8 : parts);
     const int tid = threadIdx.x;
     const int row = tid % n, part = tid / n;
     const bool active = part < parts;
@@ -2145,7 +2168,7 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
                     const float2 b = sB[c + row * LDp], v = x0[c + j * n];
                     df_mac(b.x, b.y, v.x, v.y, sh, sl);
                 }
-                red[8 * nk + (part * k + j) * n + row] = make_float2(sh, sl);
+                redu[(part * k + j) * n + row] = make_float2(sh, sl);
             }
             if (with_norm) {
                 float sbt = 0.0f;
@@ -2167,7 +2190,7 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
             df_add(-su[o].x, -su[o].y, rh, rl);
             if (has_b)
                 for (int q = 0; q < parts; ++q) {
-                    const float2 u = red[8 * nk + (q * k + j) * n + rr];
+                    const float2 u = redu[(q * k + j) * n + rr];
                     df_add(u.x, u.y, uh, ul);
                 }
             float res_f;
@@ -2211,16 +2234,14 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
     }
 }
 
-template <class Tr>
-__global__ void __launch_bounds__(RES_THREADS, 3) residual_df_kernel(const double *__restrict__ A,
-                                                                  const double *__restrict__ B,
-                                                                  const double *__restrict__ x,
-                                                                  const double *__restrict__ d, Tr *__restrict__ r,
-                                                                  long long N, int n, int ktot, int j0, int k,
-                                                                  long long per_cta, int with_norm, DevStatus *st)
+template <class Tr, int THREADS>
+__global__ void __launch_bounds__(THREADS, THREADS == 256 ? 3 : 1)
+    residual_df_kernel(const double *__restrict__ A, const double *__restrict__ B, const double *__restrict__ x,
+                       const double *__restrict__ d, Tr *__restrict__ r, long long N, int n, int ktot, int j0, int k,
+                       long long per_cta, int with_norm, DevStatus *st)
 {
     const long long b0 = (long long)blockIdx.x * per_cta;
-    residual_body_df<Tr>(A, B, x, d, r, N, n, ktot, j0, k, b0, b0 + per_cta, with_norm, st);
+    residual_body_df<Tr, THREADS>(A, B, x, d, r, N, n, ktot, j0, k, b0, b0 + per_cta, with_norm, st);
 }
 
 // many systems: one CTA per (system, block range) item
@@ -2236,14 +2257,15 @@ struct ResidualDesc {
     DevStatus *st;
 };
 
-template <class Tr>
-__global__ void __launch_bounds__(RES_THREADS, 3) residual_batch_kernel(const ResidualDesc<Tr> *__restrict__ descs,
-                                                                       const WorkItem *__restrict__ items)
+template <class Tr, int THREADS>
+__global__ void __launch_bounds__(THREADS, THREADS == 256 ? 3 : 1)
+    residual_batch_kernel(const ResidualDesc<Tr> *__restrict__ descs, const WorkItem *__restrict__ items)
 {
     const WorkItem w = items[blockIdx.x];
     const ResidualDesc<Tr> g = descs[w.desc];
     const long long b0 = (long long)w.p * g.per_cta;
-    residual_body_df<Tr>(g.A, g.B, g.x, g.d, g.r, g.N, g.n, g.k, g.j0, g.kc, b0, b0 + g.per_cta, g.norm, g.st);
+    residual_body_df<Tr, THREADS>(g.A, g.B, g.x, g.d, g.r, g.N, g.n, g.k, g.j0, g.kc, b0, b0 + g.per_cta, g.norm,
+                                  g.st);
 }
 
 // one refinement decision on the device (graph mode): relative residual,

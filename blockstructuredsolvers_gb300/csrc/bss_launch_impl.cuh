@@ -197,17 +197,19 @@ cudaError_t launch_residual(const T *A, const T *B, const T *x, const T *d, Tr *
     return cudaSuccess;
 }
 
-template <class Tr>
-cudaError_t launch_residual_df(const double *A, const double *B, const double *x, const double *d, Tr *r,
-                               long long N, int n, int k, int with_norm, DevStatus *st, cudaStream_t s)
+template <class Tr, int THREADS>
+cudaError_t launch_residual_df_t(const double *A, const double *B, const double *x, const double *d, Tr *r,
+                                 long long N, int n, int k, int with_norm, DevStatus *st, cudaStream_t s)
 {
-    auto kern = residual_df_kernel<Tr>;
-    int kc = k;
-    while (kc > 1 && residual_smem_bytes<double>(n, kc) > (size_t)200 * 1024) kc = (kc + 1) / 2;
-    const size_t smem = residual_smem_bytes<double>(n, kc);
+    auto kern = residual_df_kernel<Tr, THREADS>;
+    int kc = k;  // every column in one pass when the partials fit: A and B are read once
+    while (kc > 1 && residual_df_smem_bytes<THREADS>(n, kc) > SMEM_CTA_MAX) kc = (kc + 1) / 2;
+    const size_t smem = residual_df_smem_bytes<THREADS>(n, kc);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int per_sm = ctas_per_sm(kern, RES_THREADS, smem);
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return e;
+    const int per_sm = ctas_per_sm(kern, THREADS, smem);
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -217,13 +219,22 @@ cudaError_t launch_residual_df(const double *A, const double *B, const double *x
     grid = (N + per_cta - 1) / per_cta;
     for (int j0 = 0; j0 < k; j0 += kc) {
         const int kk = (k - j0 < kc) ? k - j0 : kc;
-        kern<<<(unsigned)grid, RES_THREADS, smem, s>>>(A, B, x, d, r, N, n, k, j0, kk, per_cta,
-                                                       (with_norm && j0 == 0) ? with_norm : 0, st);
+        kern<<<(unsigned)grid, THREADS, smem, s>>>(A, B, x, d, r, N, n, k, j0, kk, per_cta,
+                                                   (with_norm && j0 == 0) ? with_norm : 0, st);
         count_launch();
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+template <class Tr>
+cudaError_t launch_residual_df(const double *A, const double *B, const double *x, const double *d, Tr *r,
+                               long long N, int n, int k, int with_norm, DevStatus *st, cudaStream_t s)
+{
+    if (res_df_threads(n) == 512)
+        return launch_residual_df_t<Tr, 512>(A, B, x, d, r, N, n, k, with_norm, st, s);
+    return launch_residual_df_t<Tr, 256>(A, B, x, d, r, N, n, k, with_norm, st, s);
 }
 
 template <class Tc>

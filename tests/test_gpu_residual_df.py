@@ -44,7 +44,8 @@ def _run(method, A, B, x, d):
 
 
 @pytest.mark.parametrize("N,n,k", [(1, 16, 1), (2, 64, 1), (37, 64, 3), (300, 64, 1), (50, 128, 2), (20, 16, 5),
-                                   (64, 32, 4), (9, 48, 8), (40, 96, 1), (11, 8, 16)])
+                                   (64, 32, 4), (9, 48, 8), (40, 96, 1), (11, 8, 16), (33, 128, 4),
+                                   (12, 128, 8), (25, 96, 4)])
 def test_double_float_residual_matches_fp64(N, n, k):
     A, B, x, d = _system(N, n, k, seed=N * 1000 + n * 10 + k)
     r_np = d - O.block_matvec(A, B, x)
