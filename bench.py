@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--case", default=None,
                     help="run one small named case for a profiler and exit: "
                          "chain_n64 (N=4096, n=64, mixed), wide_n128 (N=2048, n=128, mixed), "
+                         "headline_eager (N=16384, n=64, mixed, no CUDA graphs: every kernel a launch), "
                          "batch_small (64 uneven systems, mixed), batch_2048 (the 2048-system batch, mixed)")
     return ap.parse_args()
 
@@ -888,10 +889,17 @@ def roofline_chain_factor(bss, A, B, d, hbm_gbs, peak_kind):
     alg_bytes = interior * (2 * nn * 8 + 3 * nn * 4) + (Q.value + 1) * nn * 8
     ms = statistics.median(ts)
     ach = alg_bytes / (ms * 1e-3) / 1e9
+    # DRAM bytes (read + write) of this kernel from one ncu capture of the same
+    # launch at N=4096 (profiles/chain_factor_mixed_N4096_n64.md: 263.5 + 157.6 MB
+    # over 3791 interior blocks), scaled by interior blocks: the traffic of a
+    # chain grows in proportion to its blocks
+    traffic = (263.529984e6 + 157.616384e6) / 3791 * interior
     return {"kernel": "chain_factor_kernel<double,float,64> (level 0) + assemble_schur", "bound": "hbm",
             "achieved": ach, "peak": hbm_gbs, "unit": "GB/s", "frac": ach / hbm_gbs,
             "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})", "duration_ms": ms,
-            "algorithmic_bytes": alg_bytes, "partitions": Q.value, "traffic": None,
+            "algorithmic_bytes": alg_bytes, "partitions": Q.value, "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the N=4096 capture, "
+                              "scaled by interior blocks",
             "note": "latency/FMA-bound chain: the HBM fraction is low by construction"}
 
 
@@ -902,13 +910,14 @@ def run_case(name, reps=3):
     import blockstructuredsolvers_gb300 as bss
     dev = torch.device("cuda", 0)
     g = torch.Generator(device=dev).manual_seed(5)
-    if name in ("chain_n64", "wide_n128"):
-        N, n = (4096, 64) if name == "chain_n64" else (2048, 128)
+    if name in ("chain_n64", "wide_n128", "headline_eager"):
+        N, n = {"chain_n64": (4096, 64), "wide_n128": (2048, 128), "headline_eager": (N_BLK, N_SZ)}[name]
         G = torch.randn((N, n, n), dtype=torch.float64, device=dev, generator=g)
         A = (G @ G.transpose(1, 2) + n * torch.eye(n, dtype=torch.float64, device=dev)).permute(1, 2, 0)
         B = torch.randn((N - 1, n, n), dtype=torch.float64, device=dev, generator=g).permute(1, 2, 0)
         d = torch.rand((N, n, 1), dtype=torch.float64, device=dev, generator=g).permute(1, 2, 0)
-        data = bss.initialize_batched(N, n, torch.float64, precision="mixed")
+        data = bss.initialize_batched(N, n, torch.float64, precision="mixed",
+                                      use_graphs=name != "headline_eager")
         data.A_tensor[:, :, :N].copy_(A)
         data.B_tensor[:, :, :N - 1].copy_(B)
         for _ in range(reps):
