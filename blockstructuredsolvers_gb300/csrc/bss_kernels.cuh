@@ -292,14 +292,15 @@ __device__ __forceinline__ T safe_pivot(T p)
 // On entry sS holds S; only its upper triangle is read (as LAPACK potrf 'U'
 // in the reference's backbone_cpu.jl:7,13 / cusolverDnXpotrf(Batched) 'U').
 // On exit sS's upper triangle holds U (U^T U = S), its lower triangle is
-// scratch, and sV holds V = U^{-1} (upper, zeros below the diagonal -- the
-// caller zeroes sV's strictly lower tiles once).
+// left as it came, and sV holds V = U^{-1} (upper, zeros below the diagonal
+// -- the caller zeroes sV's strictly lower tiles once).
 // Panels are PB = 16 wide: one warp factors each
 // PB x PB diagonal tile with shuffles (lane r owns column r; the diagonal is
 // carried in its own register so the pivot chain is shuffle -> rsqrt -> fma),
 // another warp inverts it by per-lane back substitution while the rest of
-// the CTA solves the row panel; the trailing update and the NB/PB-1 block
-// stages of V are spread over the CTA.  The helpers are kept out of line:
+// the CTA solves the row panel; the trailing update is spread over the CTA,
+// and V's off-diagonal block columns are formed by the other warps while
+// warp 0 factors the next diagonal tile.  The helpers are kept out of line:
 // inlined together into the chain kernel they push arrays to local memory.
 // ---------------------------------------------------------------------------
 
@@ -421,53 +422,49 @@ __device__ __noinline__ void trailing_update(T *sS, int o, int tid, int nthr)
     }
 }
 
-// off-diagonal tiles of V = U^{-1}:  V_IJ = -V_II sum_{P=I+1..J} U_IP V_PJ,
-// one super-diagonal stage at a time (s = J - I).  T_IJ is kept in the
-// (scratch) lower tile (J, I) of sS.
-template <class T, int LD, int NB, int PB>
-__device__ __noinline__ void inverse_stages(T *sS, T *sV, int tid, int nthr)
+// Off-diagonal block column J of V = U^{-1} (rows I < J), from V U = I:
+//   V_IJ = -(sum_{P=I..J-1} V_IP U_PJ) V_JJ
+// Needs U's block rows above J (final once their row panels are solved) and
+// V's block columns left of J, so it runs while the next diagonal tile is
+// being factored.  One thread per row (I, a): the 16 sums T(a, :) in
+// registers, then the row of -T V_JJ.
+template <class T, int LD, int PB>
+__device__ __noinline__ void inv_column(const T *sS, T *sV, int J, int t0, int nthr)
 {
-    constexpr int KP = NB / PB;
-#pragma unroll 1
-    for (int s = 1; s < KP; ++s) {
-        const int ntile = KP - s;
-        for (int e = tid; e < ntile * PB * PB; e += nthr) {
-            const int tile = e / (PB * PB), w = e - tile * PB * PB;
-            const int a = w % PB, b = w / PB;
-            const int I = tile, J = tile + s;
-            T acc0 = T(0), acc1 = T(0);
-            for (int P = I + 1; P <= J; ++P)
+    for (int e = t0; e < J * PB; e += nthr) {
+        const int I = e / PB, a = e - I * PB;
+        T t[PB];
 #pragma unroll
-                for (int q = 0; q < PB; q += 2) {
-                    acc0 = fma(sS[(PB * I + a) + (PB * P + q) * LD], sV[(PB * P + q) + (PB * J + b) * LD], acc0);
-                    acc1 = fma(sS[(PB * I + a) + (PB * P + q + 1) * LD], sV[(PB * P + q + 1) + (PB * J + b) * LD],
-                               acc1);
-                }
-            sS[(PB * J + a) + (PB * I + b) * LD] = acc0 + acc1;
-        }
-        __syncthreads();
-        for (int e = tid; e < ntile * PB * PB; e += nthr) {
-            const int tile = e / (PB * PB), w = e - tile * PB * PB;
-            const int a = w % PB, b = w / PB;
-            const int I = tile, J = tile + s;
+        for (int c = 0; c < PB; ++c) t[c] = T(0);
+        for (int P = I; P < J; ++P)
+#pragma unroll 4
+            for (int q = 0; q < PB; ++q) {
+                const T v = sV[(PB * I + a) + (PB * P + q) * LD];  // V_IP(a, q)
+#pragma unroll
+                for (int c = 0; c < PB; ++c) t[c] = fma(v, sS[(PB * P + q) + (PB * J + c) * LD], t[c]);  // U_PJ(q, c)
+            }
+#pragma unroll 4
+        for (int b = 0; b < PB; ++b) {
             T acc0 = T(0), acc1 = T(0);
-            for (int c = a; c < PB; c += 2) {
-                acc0 = fma(sV[(PB * I + a) + (PB * I + c) * LD], sS[(PB * J + c) + (PB * I + b) * LD], acc0);
-                if (c + 1 < PB)
-                    acc1 = fma(sV[(PB * I + a) + (PB * I + c + 1) * LD], sS[(PB * J + c + 1) + (PB * I + b) * LD],
-                               acc1);
+#pragma unroll
+            for (int c = 0; c < PB; c += 2) {
+                acc0 = fma(t[c], sV[(PB * J + c) + (PB * J + b) * LD], acc0);
+                acc1 = fma(t[c + 1], sV[(PB * J + c + 1) + (PB * J + b) * LD], acc1);
             }
             sV[(PB * I + a) + (PB * J + b) * LD] = -(acc0 + acc1);
         }
-        __syncthreads();
     }
 }
 
 // Factor the tile in sS into sV = U^{-1}.  Returns nonzero (in every thread)
-// if a pivot failed.  Ends with a __syncthreads.
+// if a pivot failed.  Ends with a __syncthreads.  Per panel K: warp 0
+// factors the diagonal tile while the other warps form V's block column
+// K-1; then warp 1 inverts the diagonal tile while the rest solve the row
+// panel; then the trailing update.  V's last block column follows the loop.
 template <class T, int NB, int THREADS>
 __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sflag, int tid)
 {
+    static_assert(THREADS > 32, "two warps at least");
     constexpr int LD = Geo<T, NB>::LD;
     constexpr int PB = Panel<NB>::PB;
     constexpr int KP = NB / PB;
@@ -479,22 +476,23 @@ __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sfla
         if (warp == 0) {
             const int bad = warp_chol<T, LD, PB>(sS, dinv, o, lane);
             if (bad && lane == 0) *sflag = 1;
+        } else if (K >= 2) {
+            inv_column<T, LD, PB>(sS, sV, K - 1, tid - 32, THREADS - 32);
         }
         __syncthreads();
-        if (warp == (THREADS > 32 ? 1 : 0)) warp_inv<T, LD, PB>(sS, dinv, sV, o, lane);
+        if (warp == 1) warp_inv<T, LD, PB>(sS, dinv, sV, o, lane);
         if (K + 1 < KP) {
-            if (THREADS > 32) {
-                const int t0 = warp == 0 ? lane : tid - 32;
-                if (warp != 1) panel_trsm<T, LD, NB, PB>(sS, dinv, o, t0, THREADS - 32);
-            } else {
-                panel_trsm<T, LD, NB, PB>(sS, dinv, o, tid, THREADS);
-            }
+            const int t0 = warp == 0 ? lane : tid - 32;
+            if (warp != 1) panel_trsm<T, LD, NB, PB>(sS, dinv, o, t0, THREADS - 32);
             __syncthreads();
             trailing_update<T, LD, NB, PB>(sS, o, tid, THREADS);
         }
         __syncthreads();
     }
-    inverse_stages<T, LD, NB, PB>(sS, sV, tid, THREADS);
+    if (KP > 1) {
+        inv_column<T, LD, PB>(sS, sV, KP - 1, tid, THREADS);
+        __syncthreads();
+    }
     return *sflag;
 }
 
