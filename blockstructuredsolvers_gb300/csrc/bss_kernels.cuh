@@ -292,7 +292,7 @@ __device__ __forceinline__ T safe_pivot(T p)
 // On entry sS holds S; only its upper triangle is read (as LAPACK potrf 'U'
 // in the reference's backbone_cpu.jl:7,13 / cusolverDnXpotrf(Batched) 'U').
 // On exit sS's upper triangle holds U (U^T U = S), its lower triangle is
-// left as it came, and sV holds V = U^{-1} (upper, zeros below the diagonal
+// scratch, and sV holds V = U^{-1} (upper, zeros below the diagonal
 // -- the caller zeroes sV's strictly lower tiles once).
 // Panels are PB = 16 wide: one warp factors each
 // PB x PB diagonal tile with shuffles (lane r owns column r; the diagonal is
@@ -422,6 +422,51 @@ __device__ __noinline__ void trailing_update(T *sS, int o, int tid, int nthr)
     }
 }
 
+// off-diagonal tiles of V = U^{-1} after the factorization (FP64 chains):
+// V_IJ = -V_II sum_{P=I+1..J} U_IP V_PJ, one super-diagonal stage at a time
+// (s = J - I), all threads on every stage; T_IJ is kept in the (scratch)
+// lower tile (J, I) of sS.  On GB300's FP64 pipe a warp-instruction costs
+// its full slot whatever lanes are active, so FP64 takes this form, whose
+// element-parallel stages skip the zero halves of the triangular tiles.
+template <class T, int LD, int NB, int PB>
+__device__ __noinline__ void inverse_stages(T *sS, T *sV, int tid, int nthr)
+{
+    constexpr int KP = NB / PB;
+#pragma unroll 1
+    for (int s = 1; s < KP; ++s) {
+        const int ntile = KP - s;
+        for (int e = tid; e < ntile * PB * PB; e += nthr) {
+            const int tile = e / (PB * PB), w = e - tile * PB * PB;
+            const int a = w % PB, b = w / PB;
+            const int I = tile, J = tile + s;
+            T acc0 = T(0), acc1 = T(0);
+            for (int P = I + 1; P <= J; ++P)
+#pragma unroll
+                for (int q = 0; q < PB; q += 2) {
+                    acc0 = fma(sS[(PB * I + a) + (PB * P + q) * LD], sV[(PB * P + q) + (PB * J + b) * LD], acc0);
+                    acc1 = fma(sS[(PB * I + a) + (PB * P + q + 1) * LD], sV[(PB * P + q + 1) + (PB * J + b) * LD],
+                               acc1);
+                }
+            sS[(PB * J + a) + (PB * I + b) * LD] = acc0 + acc1;
+        }
+        __syncthreads();
+        for (int e = tid; e < ntile * PB * PB; e += nthr) {
+            const int tile = e / (PB * PB), w = e - tile * PB * PB;
+            const int a = w % PB, b = w / PB;
+            const int I = tile, J = tile + s;
+            T acc0 = T(0), acc1 = T(0);
+            for (int c = a; c < PB; c += 2) {
+                acc0 = fma(sV[(PB * I + a) + (PB * I + c) * LD], sS[(PB * J + c) + (PB * I + b) * LD], acc0);
+                if (c + 1 < PB)
+                    acc1 = fma(sV[(PB * I + a) + (PB * I + c + 1) * LD], sS[(PB * J + c + 1) + (PB * I + b) * LD],
+                               acc1);
+            }
+            sV[(PB * I + a) + (PB * J + b) * LD] = -(acc0 + acc1);
+        }
+        __syncthreads();
+    }
+}
+
 // Off-diagonal block column J of V = U^{-1} (rows I < J), from V U = I:
 //   V_IJ = -(sum_{P=I..J-1} V_IP U_PJ) V_JJ
 // Needs U's block rows above J (final once their row panels are solved) and
@@ -458,9 +503,10 @@ __device__ __noinline__ void inv_column(const T *sS, T *sV, int J, int t0, int n
 
 // Factor the tile in sS into sV = U^{-1}.  Returns nonzero (in every thread)
 // if a pivot failed.  Ends with a __syncthreads.  Per panel K: warp 0
-// factors the diagonal tile while the other warps form V's block column
-// K-1; then warp 1 inverts the diagonal tile while the rest solve the row
-// panel; then the trailing update.  V's last block column follows the loop.
+// factors the diagonal tile while (FP32) the other warps form V's block
+// column K-1; then warp 1 inverts the diagonal tile while the rest solve the
+// row panel; then the trailing update.  V's last block column follows the
+// loop (FP32); FP64 forms V's off-diagonal tiles in stages after it.
 template <class T, int NB, int THREADS>
 __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sflag, int tid)
 {
@@ -476,7 +522,7 @@ __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sfla
         if (warp == 0) {
             const int bad = warp_chol<T, LD, PB>(sS, dinv, o, lane);
             if (bad && lane == 0) *sflag = 1;
-        } else if (K >= 2) {
+        } else if (K >= 2 && sizeof(T) == 4) {
             inv_column<T, LD, PB>(sS, sV, K - 1, tid - 32, THREADS - 32);
         }
         __syncthreads();
@@ -489,7 +535,9 @@ __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sfla
         }
         __syncthreads();
     }
-    if (KP > 1) {
+    if constexpr (sizeof(T) == 8) {
+        inverse_stages<T, LD, NB, PB>(sS, sV, tid, THREADS);
+    } else if (KP > 1) {
         inv_column<T, LD, PB>(sS, sV, KP - 1, tid, THREADS);
         __syncthreads();
     }
