@@ -890,10 +890,10 @@ def roofline_chain_factor(bss, A, B, d, hbm_gbs, peak_kind):
     ms = statistics.median(ts)
     ach = alg_bytes / (ms * 1e-3) / 1e9
     # DRAM bytes (read + write) of this kernel from one ncu capture of the same
-    # launch at N=4096 (profiles/chain_factor_mixed_N4096_n64.md: 263.5 + 157.6 MB
+    # launch at N=4096 (profiles/chain_factor_mixed_N4096_n64.md: 262.0 + 156.6 MB
     # over 3791 interior blocks), scaled by interior blocks: the traffic of a
     # chain grows in proportion to its blocks
-    traffic = (263.529984e6 + 157.616384e6) / 3791 * interior
+    traffic = (261.9712e6 + 156.595968e6) / 3791 * interior
     return {"kernel": "chain_factor_kernel<double,float,64> (level 0) + assemble_schur", "bound": "hbm",
             "achieved": ach, "peak": hbm_gbs, "unit": "GB/s", "frac": ach / hbm_gbs,
             "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})", "duration_ms": ms,
