@@ -1415,6 +1415,16 @@ __device__ __forceinline__ void nmul(const T *M1, const T *v1, const T *M2, cons
         cta_nmul_g<T>(M1, v1, M2, v2, base, out, sign, n, kc, red);
 }
 
+// Hint a block the CTA will read in its next step into L2: one prefetch per
+// 128-byte line, spread over the CTA's threads (no registers, no shared
+// memory; the addresses are those of the block itself).
+__device__ __forceinline__ void prefetch_l2(const void *p, size_t bytes)
+{
+    const char *c = static_cast<const char *>(p);
+    for (size_t o = (size_t)threadIdx.x * 128; o < bytes; o += (size_t)blockDim.x * 128)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(c + o));
+}
+
 template <class T>
 struct SolveArgs {
     const T *Af;   // V per block
@@ -1529,7 +1539,13 @@ __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long
         if (STAGED && (!seq || i < last)) async_copy(nxt + nn, g.Bf + i * (long long)nn, nn);
         if (STAGED && !seq && i < last) async_copy(nxt + 2 * nn, g.Y + (i + 1) * (long long)nn, nn);
         cp_async_commit();
-        // matrices of step i: staged in shared memory, or read straight from global memory
+        // matrices of step i: staged in shared memory, or read straight from global
+        // memory (then the next step's are hinted into L2 while this one runs)
+        if (!STAGED && i < last) {
+            prefetch_l2(g.Af + (i + 1) * (long long)nn, (size_t)nn * sizeof(T));
+            prefetch_l2(g.Bf + i * (long long)nn, (size_t)nn * sizeof(T));
+            if (!seq) prefetch_l2(g.Y + (i + 1) * (long long)nn, (size_t)nn * sizeof(T));
+        }
         const T *mV = STAGED ? cur : g.Af + i * (long long)nn;
         const T *mW = STAGED ? cur + nn : g.Bf + (i - 1) * (long long)nn;
         const T *mY = STAGED ? cur + 2 * nn : g.Y + i * (long long)nn;
@@ -1576,6 +1592,10 @@ __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long
             async_copy(srb + (cb ^ 1) * nkc, rhs_ptr<T>(g.d, i - 1, n, g.k, g.j0), nkc);
         }
         cp_async_commit();
+        if (!STAGED && i > first) {
+            prefetch_l2(g.Af + (i - 1) * (long long)nn, (size_t)nn * sizeof(T));
+            prefetch_l2(g.Bf + (i - 1) * (long long)nn, (size_t)nn * sizeof(T));
+        }
         const T *mV = STAGED ? cur : g.Af + i * (long long)nn;
         const T *mW = STAGED ? cur + nn : g.Bf + i * (long long)nn;
         if (i < last) {
@@ -1683,6 +1703,11 @@ __device__ __forceinline__ void chain_bwd_body(const SolveArgs<T> &g, const long
             async_copy(szb + (cb ^ 1) * nkc, rhs_ptr<T>(g.d, i - 1, n, g.k, g.j0), nkc);
         }
         cp_async_commit();
+        if (!STAGED && i > first) {
+            prefetch_l2(g.Af + (i - 1) * (long long)nn, (size_t)nn * sizeof(T));
+            prefetch_l2(g.Bf + (i - 1) * (long long)nn, (size_t)nn * sizeof(T));
+            prefetch_l2(g.Y + (i - 1) * (long long)nn, (size_t)nn * sizeof(T));
+        }
         const T *mV = STAGED ? cur : g.Af + i * (long long)nn;
         const T *mW = STAGED ? cur + nn : g.Bf + i * (long long)nn;
         const T *mY = STAGED ? cur + 2 * nn : g.Y + i * (long long)nn;
@@ -2177,6 +2202,11 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
         float2 *su = sub + par * nk;         // u_i
         float2 *sun = sub + (par ^ 1) * nk;  // u_{i+1}
         // phase 1: t partials from global A_i, B_i; B_i into shared memory
+        // (the next block's A and B are hinted into L2 meanwhile)
+        if (i + 1 < b1) {
+            prefetch_l2(A + (i + 1) * nn, (size_t)nn * sizeof(double));
+            if (i + 2 < N) prefetch_l2(B + (i + 1) * nn, (size_t)nn * sizeof(double));
+        }
         if (active) {
             const double *Ag = A + i * nn + row;
             const double *Bg = B + i * nn + row;
