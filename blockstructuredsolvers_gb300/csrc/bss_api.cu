@@ -406,7 +406,7 @@ extern "C" int bss_create_batched(int64_t N, int64_t n, int64_t k, int32_t dtype
     }
     if (h->opt.precision == BSS_PRECISION_MIXED && residual_smem_bytes<double>((int)n, 1) > (size_t)200 * 1024) {
         delete h;
-        return fail(BSS_ERR_UNSUPPORTED, "mixed precision supports n <= 128 (FP64 residual kernel)");
+        return fail(BSS_ERR_UNSUPPORTED, "mixed precision supports n <= 128 (the refinement residual keeps one n x n block in shared memory)");
     }
     if (h->opt.max_refine < 0) h->opt.max_refine = 0;
     h->N_user = N;

@@ -1,5 +1,4 @@
-// Kernel instantiations: FP64 factor/solve (plain FP64 and the FP64 coarsest
-// level of the mixed-precision path).
+// Kernel instantiations: FP64 factor/solve (the plain FP64 path).
 #include "bss_launch_impl.cuh"
 
 namespace bss {
