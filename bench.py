@@ -48,6 +48,7 @@ def parse():
                     help="run one small named case for a profiler and exit: "
                          "chain_n64 (N=4096, n=64, mixed), wide_n128 (N=2048, n=128, mixed), "
                          "headline_eager (N=16384, n=64, mixed, no CUDA graphs: every kernel a launch), "
+                         "csr_n64 (CSR assembly of N=4096, n=64), "
                          "batch_small (64 uneven systems, mixed), batch_2048 (the 2048-system batch, mixed)")
     return ap.parse_args()
 
@@ -925,6 +926,15 @@ def run_case(name, reps=3):
             bss.factorize_(data)
             bss.solve_(data)
         bss.synchronize(data)
+    elif name == "csr_n64":
+        # the sparse harness's CSR assembly (construct_block_tridiagonal) of N=4096 blocks of n=64
+        N, n = 4096, 64
+        G = torch.randn((N, n, n), dtype=torch.float64, device=dev, generator=g)
+        A = (G @ G.transpose(1, 2) + n * torch.eye(n, dtype=torch.float64, device=dev)).permute(1, 2, 0)
+        B = torch.randn((N - 1, n, n), dtype=torch.float64, device=dev, generator=g).permute(1, 2, 0)
+        for _ in range(reps):
+            M, _ = bss.construct_block_tridiagonal(A, B)
+            del M
     elif name in ("batch_small", "batch_2048"):
         rng = np.random.default_rng(1 if name == "batch_small" else 3)
         S = 64 if name == "batch_small" else 2048
