@@ -32,8 +32,9 @@ using namespace bss;
 
 namespace {
 
-constexpr int CSR_TILE = 32;  // tile edge of the assembly kernel
-constexpr int CSR_ROWS = 8;   // thread rows per tile (32 x 8 threads)
+constexpr int CSR_TR = 64;    // tile rows of the assembly kernel
+constexpr int CSR_TC = 32;    // tile columns (one warp across)
+constexpr int CSR_ROWS = 8;   // warps per CTA (32 x 8 threads)
 
 __host__ __device__ inline long long csr_block_row_start(long long i, long long n)
 {
@@ -62,23 +63,26 @@ __global__ void csr_rowptr_kernel(long long N, int n, int *row_ptr)
     }
 }
 
-// One CTA per 32 x 32 tile of one source block: grid = N x 3 parts x tn^2
-// tiles, parts 0 = B_{i-1}^T, 1 = A_i, 2 = B_i.  Values are written row by
-// row (coalesced along the CSR row); the column-major A_i / B_i tiles pass
-// through shared memory, while B_{i-1}^T is already row-contiguous in
-// column-major B_{i-1} and is copied directly.
+// One CTA per 64-row x 32-column tile of one source block: grid = N x 3
+// parts x ceil(n/64) x ceil(n/32) tiles, parts 0 = B_{i-1}^T, 1 = A_i, 2 = B_i.
+// Every thread issues its 8 loads before its first store (8 elements in
+// flight per thread).  Values are written row by row (coalesced along the
+// CSR row); the column-major A_i / B_i tiles pass through shared memory,
+// while B_{i-1}^T is already row-contiguous in column-major B_{i-1} and is
+// copied directly.
 template <class T>
-__global__ void __launch_bounds__(CSR_TILE *CSR_ROWS)
+__global__ void __launch_bounds__(CSR_TC *CSR_ROWS)
     csr_values_kernel(long long N, int n, const T *__restrict__ A, const T *__restrict__ B, int *__restrict__ col,
                       T *__restrict__ val, int write_idx)
 {
-    __shared__ T tile[CSR_TILE][CSR_TILE + 1];
-    const int tn = (n + CSR_TILE - 1) / CSR_TILE;
+    constexpr int PER = CSR_TR / CSR_ROWS;  // elements per thread
+    __shared__ T tile[CSR_TC][CSR_TR + 1];
+    const int tnr = (n + CSR_TR - 1) / CSR_TR, tnc = (n + CSR_TC - 1) / CSR_TC;
     long long t = blockIdx.x;
-    const int tc = (int)(t % tn);
-    t /= tn;
-    const int tr = (int)(t % tn);
-    t /= tn;
+    const int tc = (int)(t % tnc);
+    t /= tnc;
+    const int tr = (int)(t % tnr);
+    t /= tnr;
     const int part = (int)(t % 3);
     const long long i = t / 3;
     if (i >= N || (part == 0 && i == 0) || (part == 2 && i == N - 1)) return;
@@ -88,31 +92,44 @@ __global__ void __launch_bounds__(CSR_TILE *CSR_ROWS)
     const long long start = csr_block_row_start(i, n);
     const long long pofs = part == 0 ? 0 : (part == 1 ? (i > 0 ? n : 0) : (i > 0 ? 2 * n : n));
     const long long cbase = (i + part - 1) * n;
-    const int tx = threadIdx.x % CSR_TILE, ty = threadIdx.x / CSR_TILE;
-    const int r0 = tr * CSR_TILE, c0 = tc * CSR_TILE;
+    const int tx = threadIdx.x % CSR_TC, ty = threadIdx.x / CSR_TC;
+    const int r0 = tr * CSR_TR, c0 = tc * CSR_TC;
     if (part == 0) {
         // value (r, c) = B_{i-1}(c, r) = S[c + r n]: contiguous in c
-        for (int j = ty; j < CSR_TILE; j += CSR_ROWS) {
-            const int r = r0 + j, c = c0 + tx;
+        T v[PER];
+        const int c = c0 + tx;
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int r = r0 + ty + CSR_ROWS * q;
+            if (r < n && c < n) v[q] = S[c + (long long)r * n];
+        }
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int r = r0 + ty + CSR_ROWS * q;
             if (r < n && c < n) {
                 const long long pos = start + r * L + pofs + c;
-                val[pos] = S[c + (long long)r * n];
+                val[pos] = v[q];
                 if (write_idx) col[pos] = (int)(cbase + c);
             }
         }
         return;
     }
-    // value (r, c) = S[r + c n]: load coalesced along r, write along c
-    for (int j = ty; j < CSR_TILE; j += CSR_ROWS) {
-        const int c = c0 + j, r = r0 + tx;
-        if (r < n && c < n) tile[j][tx] = S[r + (long long)c * n];
+    // value (r, c) = S[r + c n]: load coalesced along r (two 32-row halves),
+    // write along c
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int cl = ty + CSR_ROWS * (q >> 1), rl = tx + 32 * (q & 1);
+        const int r = r0 + rl, c = c0 + cl;
+        if (r < n && c < n) tile[cl][rl] = S[r + (long long)c * n];
     }
     __syncthreads();
-    for (int j = ty; j < CSR_TILE; j += CSR_ROWS) {
-        const int r = r0 + j, c = c0 + tx;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int rl = ty + CSR_ROWS * q;
+        const int r = r0 + rl, c = c0 + tx;
         if (r < n && c < n) {
             const long long pos = start + r * L + pofs + c;
-            val[pos] = tile[tx][j];
+            val[pos] = tile[tx][rl];
             if (write_idx) col[pos] = (int)(cbase + c);
         }
     }
@@ -129,9 +146,8 @@ int assemble(long long N, int n, const T *A, const T *B, int *row_ptr, int *col,
         count_launch();
         BSS_CUDA(cudaGetLastError());
     }
-    const long long tn = (n + CSR_TILE - 1) / CSR_TILE;
-    const long long tiles = N * 3 * tn * tn;
-    csr_values_kernel<T><<<(unsigned)tiles, CSR_TILE * CSR_ROWS, 0, s>>>(N, n, A, B, col, val, write_idx ? 1 : 0);
+    const long long tiles = N * 3 * ((n + CSR_TR - 1) / CSR_TR) * ((n + CSR_TC - 1) / CSR_TC);
+    csr_values_kernel<T><<<(unsigned)tiles, CSR_TC * CSR_ROWS, 0, s>>>(N, n, A, B, col, val, write_idx ? 1 : 0);
     count_launch();
     BSS_CUDA(cudaGetLastError());
     return BSS_OK;
