@@ -1,5 +1,5 @@
 """Benchmark: factorize! + solve! of one block-tridiagonal SPD system,
-N = 16384 blocks of n = 64, k = 1 right-hand side (BASELINE config 1:
+N = 16384 blocks of n = 64, k = 1 right-hand side (
 A_i = G G^T + n I, B_i ~ N(0,1), d ~ U[0,1), seeded, generated on the GPU).
 
 A "step" is one complete solve request: put d into the handle, factorize!,
@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="skip the secondary legs")
-    ap.add_argument("--no-extra", action="store_true", help="skip the config 2/3 and served legs")
+    ap.add_argument("--no-extra", action="store_true", help="skip the large-system (N=65536, n=128), uneven-batch and served legs")
     ap.add_argument("--case", default=None,
                     help="run one small named case for a profiler and exit: "
                          "chain_n64 (N=4096, n=64, mixed), wide_n128 (N=2048, n=128, mixed), "
@@ -118,7 +118,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": val, "unit": "solves/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy, config 1 generator)",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy: A_i = G G^T + n I, B_i ~ N(0,1), d ~ U[0,1))",
         "config": {"workload": WORKLOAD, "N": N_BLK, "n": N_SZ, "k": K_RHS},
         "cpu_baseline": {"value": val, "unit": "solves/s", "cores": th, "kind": "port",
                          "sample": f"{args.steps} full factorize!+solve! of the workload, OpenBLAS "
@@ -534,8 +534,8 @@ def run_ours(args):
     if not args.quick and not args.no_extra:
         del A, B, d
         torch.cuda.empty_cache()
-        others["config2_single_system"] = run_config2(bss, dev)
-        others["uneven_batch"] = run_config3(bss, dev)
+        others["large_system_n128"] = run_large_system(bss, dev)
+        others["uneven_batch"] = run_uneven_batch(bss, dev)
         others["served_kalman"] = run_served_legs(bss)
 
     if rank == 0:
@@ -543,7 +543,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 factor + f64 refinement",
-            "data": "synthetic (seeded torch generator on device, config 1 distribution)",
+            "data": "synthetic (seeded torch generator on device: A_i = G G^T + n I, B_i ~ N(0,1), d ~ U[0,1))",
             "config": {"workload": WORKLOAD, "N": N_BLK, "n": N_SZ, "k": K_RHS, "precision": "mixed",
                        "levels": info["levels"], "coarsest_blocks": info["coarsest_blocks"],
                        "l2": "inputs (1.07 GB FP64 A,B) larger than L2; no flush",
@@ -563,7 +563,7 @@ def run_ours(args):
 
 
 # --------------------------------------------------------------------------
-# served Kalman-smoother request stream (config 4)
+# served Kalman-smoother request stream
 # --------------------------------------------------------------------------
 KF_SIZES = (8, 16, 32, 64)
 
@@ -695,7 +695,7 @@ def run_served(bss, precision, models, reqs, budget=100 * 10**9, streams=8):
 
 
 # --------------------------------------------------------------------------
-# config 2 (one large system, wide blocks) and config 3 (uneven batch)
+# one large system of wide blocks (N=65536, n=128, k=4) and the uneven batch of 2048 systems
 # --------------------------------------------------------------------------
 def _orthogonal(G):
     """Q of the QR factorization of G (positive diagonal R) by CholeskyQR2:
@@ -708,7 +708,7 @@ def _orthogonal(G):
     return Q
 
 
-def gen_config2(dev, N=65536, n=128, k=4, seed=2):
+def gen_logspectrum(dev, N=65536, n=128, k=4, seed=2):
     """A_i = Q_i diag(lambda) Q_i^T (lambda log-spaced over [1, 1e4]),
     B_i = 0.45 U_i V_i^T, d ~ N(0,1); Q, U, V orthogonal factors of
     Gaussian matrices.  Column-major (n, n, N) views."""
@@ -765,9 +765,9 @@ def _timed_handle_leg(bss, A, B, d, precision, reps):
             "refine_steps": info["refine_steps"], "levels": info["levels"]}
 
 
-def run_config2(bss, dev):
+def run_large_system(bss, dev):
     import torch
-    A, B, d = gen_config2(dev)
+    A, B, d = gen_logspectrum(dev)
     out = {"workload": "N=65536, n=128, k=4, A_i=Q diag(logspace(0,4)) Q^T, B_i=0.45 U V^T, d~N(0,1)",
            "mixed": _timed_handle_leg(bss, A, B, d, "mixed", 3),
            "plain_fp64": _timed_handle_leg(bss, A, B, d, "plain", 1)}
@@ -777,7 +777,7 @@ def run_config2(bss, dev):
     return out
 
 
-def run_config3(bss, dev, steps=3, seed=3):
+def run_uneven_batch(bss, dev, steps=3, seed=3):
     """2048 independent systems, N ~ U{16..1024}, n from {16,32,48,64,96,128},
     k ~ U{1..8}, A_i = G G^T + 2n I, B_i ~ 0.5 N(0,1), d ~ U[0,1); mixed
     precision, one batch (graph-replayed after the first call)."""

@@ -1,7 +1,7 @@
 /*
  * CPU oracle: sequential block Cholesky of a block-tridiagonal SPD matrix.
  *
- * TEST INFRASTRUCTURE ONLY.  Used by tests/ as the checker and by bench.py as
+ * TEST INFRASTRUCTURE ONLY.  Used by tests/ to check results and by bench.py as
  * the timed CPU baseline (the reference's own CPU path); never linked into or
  * called by the product library.
  *

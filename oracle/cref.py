@@ -1,6 +1,6 @@
 """ctypes driver for the C oracle (``oracle/bss_oracle.c``).
 
-TEST INFRASTRUCTURE ONLY: used by tests/ as the checker and by bench.py as the
+TEST INFRASTRUCTURE ONLY: used by tests/ to check results and by bench.py as the
 timed CPU baseline (BlockStructuredSolvers.jl src/cpu.jl:30-50 ->
 src/backbone_cpu.jl:5-33 restated in C).  Builds into ``oracle/_build/``.
 

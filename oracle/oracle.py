@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the product path imports this module:
 only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` /
-``--impl reference`` legs of ``bench.py`` may use it, and only as the checker
+``--impl reference`` legs of ``bench.py`` may use it, and only to check results
 or as the timed CPU baseline.
 
 What it restates (reference = BlockStructuredSolvers.jl, Julia):
@@ -187,10 +187,10 @@ def gen_golden_system(seed: int, N: int, n: int, k: int = 1):
     return A, B, x, d
 
 
-def gen_config0_family(rng: np.random.Generator, N: int, n: int, k: int = 1,
+def gen_shifted_family(rng: np.random.Generator, N: int, n: int, k: int = 1,
                        diag_shift: float | None = None, b_scale: float = 1.0,
                        rhs: str = "uniform"):
-    """BASELINE configs 0/1/3 family with numpy's Generator:
+    """The G G^T + shift family (the reference tests' generator) with numpy's Generator:
     A_i = G G^T + shift*I (shift = n by default), B_i = b_scale*N(0,1),
     d ~ U[0,1) n x k (rhs='uniform') or d ~ N(0,1) (rhs='normal')."""
     shift = float(n if diag_shift is None else diag_shift)
@@ -211,9 +211,9 @@ def _rand_orth(rng, count, n):
     return Q * s[:, None, :]
 
 
-def gen_config2(rng: np.random.Generator, N: int, n: int, k: int = 4,
+def gen_logspectrum(rng: np.random.Generator, N: int, n: int, k: int = 4,
                 lam_min: float = 1.0, lam_max: float = 1e4):
-    """BASELINE config 2: A_i = Q_i diag(lambda) Q_i^T, lambda log-spaced over
+    """Wide-block workload: A_i = Q_i diag(lambda) Q_i^T, lambda log-spaced over
     [lam_min, lam_max]; B_i = 0.45*lam_min*U_i V_i^T (U, V random orthogonal);
     d ~ N(0,1) n x k.  ||B_i|| = 0.45 lam_min so A is SPD by diagonal dominance
     of the spectrum (lambda_min(A) >= lam_min - 2*0.45*lam_min)."""
@@ -229,7 +229,7 @@ def gen_config2(rng: np.random.Generator, N: int, n: int, k: int = 4,
 
 
 def gen_kalman_model(rng: np.random.Generator, N: int, n: int, k: int = 1):
-    """BASELINE config 4 model (Kalman-smoother normal equations):
+    """Kalman-smoother workload model (normal equations):
     F ~ N(0,1) rescaled to spectral radius 0.95, H ~ N(0,1) (n/2 x n),
     Q = 0.1 I, R = 0.5 I, k observation sequences Y (N, m, k) simulated from
     the model (benchmark/benchmark_kf.jl:79-102 form).  Returns
@@ -248,7 +248,7 @@ def gen_kalman_model(rng: np.random.Generator, N: int, n: int, k: int = 1):
 
 
 def gen_kalman(rng: np.random.Generator, N: int, n: int, k: int = 1):
-    """BASELINE config 4 blocks, uniform: A_i = Q^-1 + F^T Q^-1 F + H^T R^-1 H,
+    """Kalman-smoother workload blocks, uniform: A_i = Q^-1 + F^T Q^-1 F + H^T R^-1 H,
     B_i = -F^T Q^-1, d_i = H^T R^-1 y_i (benchmark/benchmark_kf.jl:79-102,
     147-150 form) from gen_kalman_model."""
     F, H, Qinv, Rinv, Y = gen_kalman_model(rng, N, n, k)

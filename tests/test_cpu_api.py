@@ -31,7 +31,7 @@ def _load(data, A, B, d):
 @pytest.mark.parametrize("N,n,k", [(50, 32, 1), (1, 8, 1), (2, 5, 3), (100, 16, 2)])
 def test_cpu_api_matches_oracle(bss, T, N, n, k):
     rng = np.random.default_rng(N * 31 + n)
-    A, B, d = O.gen_config0_family(rng, N, n, k, diag_shift=max(n, 12))
+    A, B, d = O.gen_shifted_family(rng, N, n, k, diag_shift=max(n, 12))
     data = bss.initialize_cpu(N, n, T, k=k)
     assert data.N == N and len(data.A_list) == N and len(data.B_list) == N - 1
     _load(data, A, B, d)
@@ -65,7 +65,7 @@ def test_cpu_api_factor_contents_match_reference_semantics(bss):
     backbone_cpu.jl's factorize."""
     rng = np.random.default_rng(3)
     N, n = 12, 9
-    A, B, d = O.gen_config0_family(rng, N, n, 1)
+    A, B, d = O.gen_shifted_family(rng, N, n, 1)
     data = bss.initialize_cpu(N, n)
     _load(data, A, B, d)
     bss.factorize_(data)
@@ -80,7 +80,7 @@ def test_cpu_api_factor_contents_match_reference_semantics(bss):
 
 def test_cpu_api_not_spd(bss):
     rng = np.random.default_rng(4)
-    A, B, d = O.gen_config0_family(rng, 10, 6, 1)
+    A, B, d = O.gen_shifted_family(rng, 10, 6, 1)
     A[4] = -np.eye(6)
     data = bss.initialize_cpu(10, 6)
     _load(data, A, B, d)

@@ -36,9 +36,9 @@ def _gen(seed, systems, family="c0"):
     out = []
     for (N, n, k) in systems:
         if family == "c0":
-            A, B, d = O.gen_config0_family(rng, N, n, k, diag_shift=max(n, 12))
+            A, B, d = O.gen_shifted_family(rng, N, n, k, diag_shift=max(n, 12))
         else:  # the uneven-batch family: A = G G^T + 2n I, B = 0.5 N(0,1)
-            A, B, d = O.gen_config0_family(rng, N, n, k, diag_shift=2.0 * max(n, 6), b_scale=0.5)
+            A, B, d = O.gen_shifted_family(rng, N, n, k, diag_shift=2.0 * max(n, 6), b_scale=0.5)
         out.append((A, B, d))
     return out
 

@@ -1,7 +1,7 @@
 """GPU parity: the sm_103a path (through the C ABI, via the Python mirror of
 initialize_batched / factorize! / solve!) against the oracle.
 
-Tolerances (the spec bar, tighter than the reference's own
+Tolerances (tighter than the reference's own
 10*sqrt(eps) of test/test_cuda.jl:119): relative error vs the CPU oracle
 (backbone_cpu.jl restated) and vs a dense FP64 Cholesky <= 1e-10 in FP64,
 <= 1e-4 in FP32; mixed precision reaches relative residual <= 1e-12.
@@ -152,7 +152,7 @@ def test_seq_api(bss):
 def test_repeat_solve_after_one_factorize(bss):
     import torch
     rng = np.random.default_rng(5)
-    A, B, d = O.gen_config0_family(rng, 200, 24, 3)
+    A, B, d = O.gen_shifted_family(rng, 200, 24, 3)
     data = bss.initialize_batched(200, 24, torch.float64, k=3)
     upload(data, A, B, d)
     bss.factorize_(data)
@@ -177,7 +177,7 @@ def test_ragged_block_sizes(bss, n):
     N = 61
     # G G^T + n I with B ~ N(0,1) is SPD only when n > 4 sqrt(n) roughly;
     # small n needs a larger shift to stay SPD
-    A, B, d = O.gen_config0_family(rng, N, n, 2, diag_shift=max(n, 12.0))
+    A, B, d = O.gen_shifted_family(rng, N, n, 2, diag_shift=max(n, 12.0))
     _, x = _run(bss, A, B, d, torch.float64)
     assert O.rel_error(x, O.cpu_solve(A, B, d)) <= TOL64
 
@@ -186,7 +186,7 @@ def test_ragged_block_sizes(bss, n):
 def test_many_rhs(bss, k):
     import torch
     rng = np.random.default_rng(k)
-    A, B, d = O.gen_config0_family(rng, 120, 16, k)
+    A, B, d = O.gen_shifted_family(rng, 120, 16, k)
     _, x = _run(bss, A, B, d, torch.float64)
     assert O.rel_error(x, O.cpu_solve(A, B, d)) <= TOL64
 
@@ -195,7 +195,7 @@ def test_many_rhs(bss, k):
 def test_partition_counts(bss, parts):
     import torch
     rng = np.random.default_rng(parts)
-    A, B, d = O.gen_config0_family(rng, 333, 8, 1)
+    A, B, d = O.gen_shifted_family(rng, 333, 8, 1)
     _, x = _run(bss, A, B, d, torch.float64, target_partitions=parts, seq_cutoff=3)
     assert O.rel_error(x, O.cpu_solve(A, B, d)) <= TOL64
 
@@ -203,7 +203,7 @@ def test_partition_counts(bss, parts):
 def test_not_spd_is_reported(bss):
     import torch
     rng = np.random.default_rng(9)
-    A, B, d = O.gen_config0_family(rng, 100, 8, 1)
+    A, B, d = O.gen_shifted_family(rng, 100, 8, 1)
     A[37] = -A[37]
     data = bss.initialize_batched(100, 8, torch.float64)
     upload(data, A, B, d)
@@ -215,11 +215,11 @@ def test_not_spd_is_reported(bss):
 
 
 def test_config2_family_mixed(bss):
-    """config 2 generator (lambda in [1, 1e4]) at a reduced size: FP32 factor
+    """log-spaced-spectrum generator (lambda in [1, 1e4]) at a reduced size: FP32 factor
     + FP64 refinement reaches 1e-12."""
     import torch
     rng = np.random.default_rng(2)
-    A, B, d = O.gen_config2(rng, 400, 32, 4)
+    A, B, d = O.gen_logspectrum(rng, 400, 32, 4)
     data, x = _run(bss, A, B, d, torch.float64, precision="mixed")
     assert bss.get_info(data)["rel_residual"] <= 1e-12
     assert O.rel_residual(A, B, x, d) <= 1e-12
@@ -237,7 +237,7 @@ def test_kalman_family(bss):
 def test_residual_entry_point(bss):
     import torch
     rng = np.random.default_rng(1)
-    A, B, d = O.gen_config0_family(rng, 64, 16, 2)
+    A, B, d = O.gen_shifted_family(rng, 64, 16, 2)
     # a perturbed solution, so the residual is well above roundoff
     x = O.cpu_solve(A, B, d) + 1e-6 * rng.standard_normal(d.shape)
     to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda().permute(1, 2, 0)
@@ -257,7 +257,7 @@ def test_residual_entry_point(bss):
 
 @pytest.mark.parametrize("T", ["f64", "f32", "mixed"])
 def test_config1_full_size_properties(bss, T):
-    """N=16384, n=64 (config 1): size-independent properties -- the relative
+    """N=16384, n=64: size-independent properties -- the relative
     residual, and agreement with an FP64 solve on a sampled subset of blocks
     checked by the block operator."""
     import torch
@@ -295,7 +295,7 @@ def test_graph_replay_matches_eager(bss, precision):
     refinement outcome must be reported after synchronize."""
     import torch
     rng = np.random.default_rng(11)
-    A, B, d = O.gen_config0_family(rng, 700, 32, 2)
+    A, B, d = O.gen_shifted_family(rng, 700, 32, 2)
     outs = []
     for use_graphs in (True, False):
         data = bss.initialize_batched(700, 32, torch.float64, k=2, precision=precision, use_graphs=use_graphs)

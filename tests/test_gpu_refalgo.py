@@ -18,7 +18,7 @@ def test_reference_algorithm_matches_oracle(N, n, k, T):
     import blockstructuredsolvers_gb300 as bss
     tdt = torch.float64 if T == "f64" else torch.float32
     rng = np.random.default_rng(N + n)
-    A, B, d = O.gen_config0_family(rng, N, n, k, diag_shift=max(n, 12))
+    A, B, d = O.gen_shifted_family(rng, N, n, k, diag_shift=max(n, 12))
     data = bss.initialize_reference_algorithm(N, n, tdt, k=k)
     upload(data, A, B, d)
     bss.factorize_(data)

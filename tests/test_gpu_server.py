@@ -45,7 +45,7 @@ def _systems(seed, shapes):
     rng = np.random.default_rng(seed)
     out = []
     for (N, n, k) in shapes:
-        A, B, d = O.gen_config0_family(rng, N, n, k, diag_shift=2.0 * max(n, 6), b_scale=0.5)
+        A, B, d = O.gen_shifted_family(rng, N, n, k, diag_shift=2.0 * max(n, 6), b_scale=0.5)
         out.append((A, B, d))
     return out
 

@@ -49,7 +49,7 @@ def test_sparse_cholesky_matches_oracle(N, n, k, T):
     import blockstructuredsolvers_gb300 as bss
     tdt = torch.float64 if T == "f64" else torch.float32
     rng = np.random.default_rng(N + 3 * n)
-    A, B, d = O.gen_config0_family(rng, N, n, k, diag_shift=max(n, 12))
+    A, B, d = O.gen_shifted_family(rng, N, n, k, diag_shift=max(n, 12))
     data = bss.initialize_sparse_cholesky(N, n, tdt, k=k)
     upload(data, A, B, d)
     bss.analyze_(data)
@@ -77,7 +77,7 @@ def test_sparse_cholesky_refactor_new_values():
     data = bss.initialize_sparse_cholesky(N, n, torch.float64, k=k)
     for seed in (1, 2):
         rng = np.random.default_rng(seed)
-        A, B, d = O.gen_config0_family(rng, N, n, k, diag_shift=16)
+        A, B, d = O.gen_shifted_family(rng, N, n, k, diag_shift=16)
         upload(data, A, B, d)
         bss.factorize_(data)
         bss.solve_(data)
@@ -93,7 +93,7 @@ def test_sparse_cholesky_not_spd_names_the_block(blk, row, val):
     import blockstructuredsolvers_gb300 as bss
     N, n = 10, 8
     rng = np.random.default_rng(0)
-    A, B, d = O.gen_config0_family(rng, N, n, 1, diag_shift=12)
+    A, B, d = O.gen_shifted_family(rng, N, n, 1, diag_shift=12)
     B[:] = 0.0
     A[blk] = np.eye(n)
     A[blk][row, row] = val

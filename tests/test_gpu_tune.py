@@ -26,7 +26,7 @@ def test_autotune_entry_is_used_and_correct(bss, tmp_path):
     assert e["single_ms"] > 0 and e["batch_ms"] > 0
     assert bss.autotune_lookup(32, torch.float64, "mixed") == e
     rng = np.random.default_rng(1)
-    A, B, d = O.gen_config0_family(rng, 3000, 32, 1)
+    A, B, d = O.gen_shifted_family(rng, 3000, 32, 1)
     data = bss.initialize_batched(3000, 32, torch.float64, precision="mixed")
     upload(data, A, B, d)
     bss.factorize_(data)

@@ -43,7 +43,7 @@ def _run(bss, A, B, d, T, **kw):
 def test_wide_fp64(bss, n):
     import torch
     rng = np.random.default_rng(100 + n)
-    A, B, d = O.gen_config0_family(rng, 37, n, 2)
+    A, B, d = O.gen_shifted_family(rng, 37, n, 2)
     _, x = _run(bss, A, B, d, torch.float64)
     assert O.rel_error(x, O.cpu_solve(A, B, d)) <= TOL64
     assert O.rel_error(x, O.dense_solve(A, B, d)) <= TOL64
@@ -53,18 +53,18 @@ def test_wide_fp64(bss, n):
 def test_wide_fp32(bss, n):
     import torch
     rng = np.random.default_rng(200 + n)
-    A, B, d = O.gen_config0_family(rng, 45, n, 1, diag_shift=2.0 * n, b_scale=0.5)
+    A, B, d = O.gen_shifted_family(rng, 45, n, 1, diag_shift=2.0 * n, b_scale=0.5)
     _, x = _run(bss, A, B, d, torch.float32)
     assert O.rel_error(x, O.cpu_solve(A, B, d)) <= TOL32
 
 
 @pytest.mark.parametrize("n", [96, 128])
 def test_wide_mixed_config2_family(bss, n):
-    """config 2 generator (lambda log-spaced over [1, 1e4]) at n = 96, 128:
+    """log-spaced-spectrum generator (lambda over [1, 1e4]) at n = 96, 128:
     FP32 factor + FP64 refinement to 1e-12."""
     import torch
     rng = np.random.default_rng(300 + n)
-    A, B, d = O.gen_config2(rng, 150, n, 4)
+    A, B, d = O.gen_logspectrum(rng, 150, n, 4)
     data, x = _run(bss, A, B, d, torch.float64, precision="mixed")
     info = bss.get_info(data)
     assert info["rel_residual"] <= 1e-12
@@ -76,7 +76,7 @@ def test_wide_mixed_config2_family(bss, n):
 def test_wide_partitions_and_reference_plan(bss, plan):
     import torch
     rng = np.random.default_rng(7)
-    A, B, d = O.gen_config0_family(rng, 130, 96, 1)
+    A, B, d = O.gen_shifted_family(rng, 130, 96, 1)
     _, x = _run(bss, A, B, d, torch.float64, plan=plan)
     assert O.rel_error(x, O.cpu_solve(A, B, d)) <= TOL64
 
@@ -84,7 +84,7 @@ def test_wide_partitions_and_reference_plan(bss, plan):
 def test_wide_seq_api(bss):
     import torch
     rng = np.random.default_rng(8)
-    A, B, d = O.gen_config0_family(rng, 20, 128, 3)
+    A, B, d = O.gen_shifted_family(rng, 20, 128, 3)
     data = bss.initialize_seq(20, 128, torch.float64, k=3)
     upload(data, A, B, d)
     bss.factorize_(data)
@@ -96,7 +96,7 @@ def test_wide_seq_api(bss):
 def test_wide_many_rhs(bss):
     import torch
     rng = np.random.default_rng(9)
-    A, B, d = O.gen_config0_family(rng, 40, 128, 40)
+    A, B, d = O.gen_shifted_family(rng, 40, 128, 40)
     _, x = _run(bss, A, B, d, torch.float64)
     assert O.rel_error(x, O.cpu_solve(A, B, d)) <= TOL64
 
@@ -104,7 +104,7 @@ def test_wide_many_rhs(bss):
 def test_wide_not_spd_is_reported(bss):
     import torch
     rng = np.random.default_rng(10)
-    A, B, d = O.gen_config0_family(rng, 50, 96, 1)
+    A, B, d = O.gen_shifted_family(rng, 50, 96, 1)
     A[21] = -np.eye(96)
     data = bss.initialize_batched(50, 96, torch.float64)
     upload(data, A, B, d)
@@ -122,7 +122,7 @@ def test_batch_with_wide_systems(bss):
                for _ in range(2)]
     probs = []
     for (N, n, k) in systems:
-        probs.append(O.gen_config0_family(rng, N, n, k, diag_shift=2.0 * n, b_scale=0.5))
+        probs.append(O.gen_shifted_family(rng, N, n, k, diag_shift=2.0 * n, b_scale=0.5))
     b = bss.initialize_multi([s[0] for s in systems], [s[1] for s in systems], [s[2] for s in systems],
                              torch.float64, precision="mixed")
     for sysv, (A, B, d) in zip(b.systems, probs):

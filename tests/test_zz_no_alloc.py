@@ -35,7 +35,7 @@ def test_noalloc_matches_handle_path_twice(T):
     code = _lib.BSS_F64 if T == "f64" else _lib.BSS_F32
     for call, (seed, N, n, k) in enumerate([(1, 300, 16, 2), (2, 250, 24, 1)]):
         rng = np.random.default_rng(seed)
-        A, B, d = O.gen_config0_family(rng, N, n, k)
+        A, B, d = O.gen_shifted_family(rng, N, n, k)
         # existing entry point
         data = bss.initialize_batched(N, n, dt, k=k)
         upload(data, A, B, d)
@@ -70,7 +70,7 @@ def test_noalloc_rejects_oversize_and_reports_not_spd():
     assert torch.count_nonzero(big).item() == 0
     # a non-SPD block is reported
     rng = np.random.default_rng(3)
-    A, B, d = O.gen_config0_family(rng, 60, 8, 1)
+    A, B, d = O.gen_shifted_family(rng, 60, 8, 1)
     A[17] = -A[17]
     Ad, Bd, dd = (_colmajor(a, torch.float64, torch) for a in (A, B, d))
     rc = L.bss_factor_solve_noalloc(60, 8, 1, _lib.BSS_F64, ctypes.c_void_p(Ad.data_ptr()),
