@@ -207,7 +207,8 @@ struct bss_spchol {
     void *A = nullptr, *B = nullptr, *d = nullptr;  // user tensors (column-major blocks)
     int *row_ptr = nullptr, *col = nullptr;
     void *val = nullptr, *rhs = nullptr, *sol = nullptr, *work = nullptr;
-    bool analyzed = false;
+    bool analyzed = false;  // symbolic phase done (pattern and workspace fixed)
+    bool factored = false;  // a numeric factorization of the current values exists
 };
 
 namespace {
@@ -224,6 +225,10 @@ template <class T>
 int sp_analyze(bss_spchol *h)
 {
     const int m = (int)(h->N * h->n);
+    h->factored = false;
+    if (h->analyzed)  // the pattern is fixed by (N, n): refresh the values only
+        return assemble<T>(h->N, (int)h->n, (const T *)h->A, (const T *)h->B, h->row_ptr, h->col, (T *)h->val, false,
+                           h->stream);
     int rc = assemble<T>(h->N, (int)h->n, (const T *)h->A, (const T *)h->B, h->row_ptr, h->col, (T *)h->val, true,
                          h->stream);
     if (rc) return rc;
@@ -254,6 +259,7 @@ int sp_factor(bss_spchol *h)
         if (rc) return rc;
     }
     int pos = -1;
+    h->factored = false;
     if constexpr (std::is_same<T, double>::value) {
         BSS_SP(cusolverSpDcsrcholFactor(h->sp, m, (int)h->nnz, h->descr, (const double *)h->val, h->row_ptr, h->col,
                                         h->info, h->work));
@@ -270,13 +276,14 @@ int sp_factor(bss_spchol *h)
         return fail(BSS_ERR_NOT_SPD, "sparse Cholesky: non-positive pivot at row " + std::to_string(row) +
                                          " (block " + std::to_string(row / h->n) + ")");
     }
+    h->factored = true;
     return BSS_OK;
 }
 
 template <class T>
 int sp_solve(bss_spchol *h)
 {
-    if (!h->analyzed) return fail(BSS_ERR_ARG, "bss_spchol_solve: not factorized");
+    if (!h->factored) return fail(BSS_ERR_STATE, "bss_spchol_solve: not factorized");
     const long long Nn = h->N * h->n;
     int rc = rhs_move<T>(h->N, (int)h->n, (int)h->k, (T *)h->d, (T *)h->rhs, true, h->stream);
     if (rc) return rc;

@@ -381,10 +381,11 @@ int bss_refalgo_solve(bss_refalgo *h);
  * csrcholFactor, csrcholSolve) over the bss_csr_assemble matrix.  Tensors
  * as for bss_create_batched without padding (A n x n x N, B n x n x (N-1),
  * d n x k x N, column-major, device); analyze assembles the CSR matrix and
- * runs the symbolic phase; factorize re-assembles the values (analyzing
- * first if needed) and factors, returning BSS_ERR_NOT_SPD on a zero pivot;
- * solve overwrites d with the solution.  The library phases synchronise the
- * stream. */
+ * runs the symbolic phase (again: refreshes the values only); factorize
+ * re-assembles the values (analyzing first if needed) and factors, returning
+ * BSS_ERR_NOT_SPD on a non-positive pivot; solve overwrites d with the
+ * solution and returns BSS_ERR_STATE unless a factorization succeeded since
+ * the last analyze.  The library phases synchronise the stream. */
 int64_t bss_csr_nnz(int64_t N, int64_t n);
 int bss_csr_assemble(int64_t N, int64_t n, int32_t dtype, const void *A, const void *B, int32_t *row_ptr,
                      int32_t *col_idx, void *vals, void *stream);

@@ -101,3 +101,25 @@ def test_sparse_cholesky_not_spd_names_the_block(blk, row, val):
     upload(data, A, B, d)
     with pytest.raises(bss.NotSPDError, match=rf"row {blk * n + row} \(block {blk}\)"):
         bss.factorize_(data)
+
+
+def test_sparse_cholesky_call_order():
+    """analyze twice keeps the analysis; solve before a successful
+    factorize is BSS_ERR_STATE; after it, the solve is correct."""
+    import torch
+    import blockstructuredsolvers_gb300 as bss
+    from blockstructuredsolvers_gb300 import _lib
+    N, n, k = 20, 8, 1
+    rng = np.random.default_rng(11)
+    A, B, d = O.gen_shifted_family(rng, N, n, k, diag_shift=12)
+    data = bss.initialize_sparse_cholesky(N, n, torch.float64, k=k)
+    upload(data, A, B, d)
+    bss.analyze_(data)
+    bss.analyze_(data)
+    with pytest.raises(bss.BSSError) as exc:
+        bss.solve_(data)
+    assert exc.value.code == _lib.BSS_ERR_STATE
+    bss.factorize_(data)
+    bss.solve_(data)
+    torch.cuda.synchronize()
+    assert O.rel_error(download_x(data, N), O.cpu_solve(A, B, d)) <= 1e-10
