@@ -140,3 +140,43 @@ extern "C" int bss_diag_residual(int64_t N, int64_t n, int64_t k, int32_t method
     if (e != cudaSuccess) return cuda_fail(e, "bss_diag_residual");
     return BSS_OK;
 }
+
+namespace {
+// an mbarrier that expects one arrival and never gets it: the bounded wait of
+// the tensor-core kernels (mbar_wait) must give up after `polls` polls and
+// say so; out[0] = 1 when it expired, out[1] = clock cycles it took
+__global__ void diag_wait_kernel(unsigned polls, long long *out)
+{
+    __shared__ __align__(8) uint64_t mbar;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const long long t0 = clock64();
+        const bool ok = mbar_wait(smem_u32(&mbar), 0u, polls);
+        out[1] = clock64() - t0;
+        out[0] = ok ? 0 : 1;
+    }
+}
+}  // namespace
+
+// Diagnostic: the bounded mbarrier wait on a barrier nothing arrives on.
+extern "C" int bss_diag_wait_timeout(int64_t polls, int64_t *timed_out, int64_t *cycles)
+{
+    if (polls < 1 || polls > (int64_t)TC_WAIT_LIMIT || !timed_out || !cycles)
+        return fail(BSS_ERR_ARG, "bss_diag_wait_timeout: bad argument");
+    long long *d = nullptr;
+    BSS_CUDA(cudaMalloc((void **)&d, 2 * sizeof(long long)));
+    diag_wait_kernel<<<1, 32>>>((unsigned)polls, d);
+    count_launch();
+    long long h[2] = {0, 0};
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "bss_diag_wait_timeout");
+    *timed_out = h[0];
+    *cycles = h[1];
+    return BSS_OK;
+}

@@ -36,7 +36,10 @@ constexpr int TC_OPERAND_BYTES = 128 * TC_K_CHUNK * 4;  // one operand part of o
 constexpr int TC_STAGE_BYTES = 4 * TC_OPERAND_BYTES;    // X hi, X lo, Y hi, Y lo
 constexpr int TC_NSTAGE = 1;  // stage buffers (one: two CTAs fit per SM)
 constexpr int TC_TMEM_COLS = 128;
-constexpr unsigned TC_WAIT_LIMIT = 1u << 22;  // try_wait polls before a stage counts as lost
+// try_wait polls before a stage counts as lost: a poll on an unfinished
+// mbarrier suspends ~7.8K SM cycles (measured), so 2^18 polls give up after
+// about one second; a stage of MMAs completes within a few polls
+constexpr unsigned TC_WAIT_LIMIT = 1u << 18;
 
 struct TcCtx {
     uint32_t taddr;      // TMEM accumulator (lane 0, first column)
@@ -96,10 +99,11 @@ __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence:
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// bounded wait for the given parity of an mbarrier; false when it expired
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+// bounded wait for the given parity of an mbarrier (at most `limit`
+// try_wait polls); false when it expired
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, unsigned limit = TC_WAIT_LIMIT)
 {
-    for (unsigned it = 0; it < TC_WAIT_LIMIT; ++it) {
+    for (unsigned it = 0; it < limit; ++it) {
         uint32_t ok;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"

@@ -419,6 +419,12 @@ int bss_diag_wide_occupancy(int64_t *out);
 int bss_diag_residual(int64_t N, int64_t n, int64_t k, int32_t method, const double *A, const double *B,
                       const double *x, const double *d, double *r, void *stream);
 
+/* Diagnostic (no counterpart in the reference): the bounded mbarrier wait of
+ * the tensor-core kernels, run on a barrier that nothing arrives on with at
+ * most `polls` (1 .. 2^18) polls.  *timed_out = 1 when the wait gave up (as
+ * it must), *cycles = the SM clock cycles it took.  Synchronises. */
+int bss_diag_wait_timeout(int64_t polls, int64_t *timed_out, int64_t *cycles);
+
 /* Number of CUDA kernels this library has launched in this process, over
  * all handles (no counterpart in the reference; benchmarks report it). */
 int64_t bss_kernel_launches(void);
