@@ -506,7 +506,9 @@ void plan_resid(Builder &B, int nb, std::vector<std::function<Step(char *)>> &ds
         if ((h->levels[0].t == F64) != std::is_same<Tr, double>::value || nb_class(h->n) != nb) continue;
         const long long per = std::max(1LL, std::min(h->N, 32LL));
         int kc = (int)h->k;  // column chunk whose shared memory fits
-        while (kc > 1 && res_smem(nb, (int)h->n, kc) > SMEM_CTA_MAX) kc = (kc + 1) / 2;
+        while (kc > 1 && res_smem(nb, (int)h->n, kc) > (nb == (int)WIDE_CLASS ? residual_df_smem_cap<512>()
+                                                                                 : residual_df_smem_cap<256>()))
+            kc = (kc + 1) / 2;
         for (int j0 = 0; j0 < h->k; j0 += kc) {
             const int kk = (int)std::min<long long>(kc, h->k - j0);
             ResidualDesc<Tr> d{(const double *)h->A, (const double *)h->B, h->x64, (const double *)h->d,

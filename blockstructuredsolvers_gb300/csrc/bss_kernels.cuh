@@ -2118,6 +2118,16 @@ constexpr size_t SMEM_CTA_MAX = 227 * 1024;
 // CTA per SM fits the staged B_i), else 256
 __host__ __device__ constexpr int res_df_threads(int n) { return n > 64 ? 512 : 256; }
 
+// largest shared memory of one residual CTA when choosing the column chunk:
+// a 256-thread CTA keeps at least two CTAs per SM (many columns in one pass
+// would leave one 8-warp CTA per SM, which costs more than re-reading A and
+// B per chunk); a 512-thread CTA may take a whole SM
+template <int THREADS>
+__host__ __device__ constexpr size_t residual_df_smem_cap()
+{
+    return THREADS == 256 ? (size_t)112 * 1024 : SMEM_CTA_MAX;
+}
+
 // shared memory of residual_body_df: staged B_i (n (n+1)), x ring (3 nk),
 // u ping-pong (2 nk) and the t / u partials (2 parts nk) as (hi, lo) pairs,
 // plus the FP32 norm partials (25 n)

@@ -203,7 +203,7 @@ cudaError_t launch_residual_df_t(const double *A, const double *B, const double 
 {
     auto kern = residual_df_kernel<Tr, THREADS>;
     int kc = k;  // every column in one pass when the partials fit: A and B are read once
-    while (kc > 1 && residual_df_smem_bytes<THREADS>(n, kc) > SMEM_CTA_MAX) kc = (kc + 1) / 2;
+    while (kc > 1 && residual_df_smem_bytes<THREADS>(n, kc) > residual_df_smem_cap<THREADS>()) kc = (kc + 1) / 2;
     const size_t smem = residual_df_smem_bytes<THREADS>(n, kc);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
