@@ -1390,6 +1390,88 @@ __device__ __forceinline__ void cta_nmul_g(const T *M1, const T *v1, const T *M2
     }
 }
 
+// Forms for a block staged in shared memory (leading dimension n, a multiple
+// of 4) and several right-hand-side columns, in FP32: every thread owns whole
+// outputs, so no cross-lane reduction is needed, and walks the contraction in
+// float4 steps; the lanes of a shared-memory wavefront start their walks at
+// different offsets (4 (lane % 8) mod n) so that they hit distinct banks.
+//
+// out(c, j) (+)= sign * sum_r M(r, c) v(r, j): thread = (column c, the
+// right-hand sides jg, jg + tpc, ... with tpc = threads / n).
+__device__ __forceinline__ void cta_tmul_s(const float *sM, const float *v, float *out, int n, int kc, float sign,
+                                           bool accumulate)
+{
+    const int tpc = (int)blockDim.x / n;
+    const int c = threadIdx.x % n, jg = threadIdx.x / n;
+    if (jg >= tpc) return;
+    const int rot = (4 * (threadIdx.x & 7)) % n;
+    const float *mc = sM + (size_t)c * n;
+    for (int j0 = jg; j0 < kc; j0 += 4 * tpc) {
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (int r4 = 0; r4 < n; r4 += 4) {
+            int r = r4 + rot;
+            if (r >= n) r -= n;
+            const float4 m = *reinterpret_cast<const float4 *>(mc + r);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int j = j0 + tpc * q;
+                if (j < kc) {
+                    const float4 x = *reinterpret_cast<const float4 *>(v + r + (size_t)j * n);
+                    acc[q] = fmaf(m.x, x.x, fmaf(m.y, x.y, fmaf(m.z, x.z, fmaf(m.w, x.w, acc[q]))));
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int j = j0 + tpc * q;
+            if (j < kc) {
+                const int o = c + j * n;
+                out[o] = accumulate ? out[o] + sign * acc[q] : sign * acc[q];
+            }
+        }
+    }
+}
+
+// out(r, j) = base(r, j) + sign * (sum_c M1(r, c) v1(c, j) [+ sum_c M2(r, c)
+// v2(c, j)]) (base may be null, may be out): thread = (row r, right-hand sides
+// jg, jg + tpc, ...); M read along rows (lanes on consecutive rows), v as
+// float4 broadcasts.  No barrier.
+__device__ __forceinline__ void cta_nmul_s(const float *M1, const float *v1, const float *M2, const float *v2,
+                                           const float *base, float *out, float sign, int n, int kc)
+{
+    const int tpc = (int)blockDim.x / n;
+    const int r = threadIdx.x % n, jg = threadIdx.x / n;
+    if (jg >= tpc) return;
+    for (int j0 = jg; j0 < kc; j0 += 4 * tpc) {
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (int mi = 0; mi < 2; ++mi) {
+            const float *M = mi == 0 ? M1 : M2;
+            const float *v = mi == 0 ? v1 : v2;
+            if (!M) continue;
+            for (int c = 0; c < n; c += 4) {
+                const float m0 = M[r + (size_t)c * n], m1 = M[r + (size_t)(c + 1) * n];
+                const float m2 = M[r + (size_t)(c + 2) * n], m3 = M[r + (size_t)(c + 3) * n];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int j = j0 + tpc * q;
+                    if (j < kc) {
+                        const float4 x = *reinterpret_cast<const float4 *>(v + c + (size_t)j * n);
+                        acc[q] = fmaf(m0, x.x, fmaf(m1, x.y, fmaf(m2, x.z, fmaf(m3, x.w, acc[q]))));
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int j = j0 + tpc * q;
+            if (j < kc) {
+                const int o = r + j * n;
+                out[o] = (base ? base[o] : 0.0f) + sign * acc[q];
+            }
+        }
+    }
+}
+
 // Staged blocks: the transpose product takes the register-blocked form when
 // there are several right-hand-side columns (every matrix element reused
 // across them; lanes run along rows, conflict-free on shared memory, no
@@ -1399,20 +1481,35 @@ __device__ __forceinline__ void cta_nmul_g(const T *M1, const T *v1, const T *M2
 template <bool STAGED, class T>
 __device__ __forceinline__ void tmul(const T *M, const T *v, T *out, int n, int kc, T sign, bool accumulate)
 {
+    if constexpr (STAGED && std::is_same<T, float>::value) {
+        if (kc > 1 && (n & 3) == 0 && n <= (int)blockDim.x) {
+            cta_tmul_s(M, v, out, n, kc, sign, accumulate);
+            return;
+        }
+    }
     if (STAGED && kc == 1)
         cta_tmul<T>(M, v, out, n, kc, sign, accumulate);
     else
         cta_tmul_g<T>(M, v, out, n, kc, sign, accumulate);
 }
 
+// the staged multi-column form when there are more outputs than threads (else
+// the split contraction of cta_nmul keeps every thread busy)
 template <bool STAGED, class T>
 __device__ __forceinline__ void nmul(const T *M1, const T *v1, const T *M2, const T *v2, const T *base, T *out,
                                      T sign, int n, int kc, T *red)
 {
-    if constexpr (STAGED)
+    if constexpr (STAGED) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (kc > 1 && (n & 3) == 0 && n * kc > (int)blockDim.x) {
+                cta_nmul_s(M1, v1, M2, v2, base, out, sign, n, kc);
+                return;
+            }
+        }
         cta_nmul<T>(M1, v1, M2, v2, base, out, sign, n, kc, red);
-    else
+    } else {
         cta_nmul_g<T>(M1, v1, M2, v2, base, out, sign, n, kc, red);
+    }
 }
 
 // Hint a block the CTA will read in its next step into L2: one prefetch per
