@@ -85,3 +85,13 @@ def test_no_gpu_is_an_error_not_a_fallback(lib):
     rc = lib.bss_create_batched(50, 8, 1, _lib.BSS_F64, None, None, ctypes.byref(h))
     assert rc in (_lib.BSS_ERR_CUDA, _lib.BSS_ERR_OOM)
     assert not h.value
+
+
+def test_csr_nnz_host_only():
+    """bss_csr_nnz is host arithmetic (no GPU needed): n^2 (3N - 2) entries,
+    -1 for empty shapes."""
+    from blockstructuredsolvers_gb300 import _lib
+    L = _lib.load()
+    for N, n in [(1, 4), (2, 3), (16384, 64), (100, 32)]:
+        assert L.bss_csr_nnz(N, n) == n * n * (3 * N - 2)
+    assert L.bss_csr_nnz(0, 4) == -1 and L.bss_csr_nnz(4, 0) == -1
