@@ -1391,34 +1391,34 @@ __device__ __forceinline__ void cta_nmul_g(const T *M1, const T *v1, const T *M2
 }
 
 // Forms for a block staged in shared memory (leading dimension n, a multiple
-// of 4) and several right-hand-side columns, in FP32: every thread owns whole
-// outputs, so no cross-lane reduction is needed, and walks the contraction in
-// float4 steps; the lanes of a shared-memory wavefront start their walks at
-// different offsets (4 (lane % 8) mod n) so that they hit distinct banks.
+// of the vector width W: 4 floats or 2 doubles, 16 bytes) and several
+// right-hand-side columns: every thread owns whole outputs, so no cross-lane
+// reduction is needed, and walks the contraction in 16-byte steps; the lanes
+// of a shared-memory wavefront start their walks at different offsets
+// (W (lane % 8) mod n) so that they hit distinct banks.
 //
 // out(c, j) (+)= sign * sum_r M(r, c) v(r, j): thread = (column c, the
 // right-hand sides jg, jg + tpc, ... with tpc = threads / n).
-__device__ __forceinline__ void cta_tmul_s(const float *sM, const float *v, float *out, int n, int kc, float sign,
-                                           bool accumulate)
+template <class T>
+__device__ __forceinline__ void cta_tmul_s(const T *sM, const T *v, T *out, int n, int kc, T sign, bool accumulate)
 {
+    using VT = typename Vec<T>::type;
+    constexpr int W = Vec<T>::W;
     const int tpc = (int)blockDim.x / n;
     const int c = threadIdx.x % n, jg = threadIdx.x / n;
     if (jg >= tpc) return;
-    const int rot = (4 * (threadIdx.x & 7)) % n;
-    const float *mc = sM + (size_t)c * n;
+    const int rot = (W * (threadIdx.x & 7)) % n;
+    const T *mc = sM + (size_t)c * n;
     for (int j0 = jg; j0 < kc; j0 += 4 * tpc) {
-        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        for (int r4 = 0; r4 < n; r4 += 4) {
+        T acc[4] = {T(0), T(0), T(0), T(0)};
+        for (int r4 = 0; r4 < n; r4 += W) {
             int r = r4 + rot;
             if (r >= n) r -= n;
-            const float4 m = *reinterpret_cast<const float4 *>(mc + r);
+            const VT m = *reinterpret_cast<const VT *>(mc + r);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int j = j0 + tpc * q;
-                if (j < kc) {
-                    const float4 x = *reinterpret_cast<const float4 *>(v + r + (size_t)j * n);
-                    acc[q] = fmaf(m.x, x.x, fmaf(m.y, x.y, fmaf(m.z, x.z, fmaf(m.w, x.w, acc[q]))));
-                }
+                if (j < kc) fma_vec(acc[q], m, *reinterpret_cast<const VT *>(v + r + (size_t)j * n));
             }
         }
 #pragma unroll
@@ -1435,28 +1435,34 @@ __device__ __forceinline__ void cta_tmul_s(const float *sM, const float *v, floa
 // out(r, j) = base(r, j) + sign * (sum_c M1(r, c) v1(c, j) [+ sum_c M2(r, c)
 // v2(c, j)]) (base may be null, may be out): thread = (row r, right-hand sides
 // jg, jg + tpc, ...); M read along rows (lanes on consecutive rows), v as
-// float4 broadcasts.  No barrier.
-__device__ __forceinline__ void cta_nmul_s(const float *M1, const float *v1, const float *M2, const float *v2,
-                                           const float *base, float *out, float sign, int n, int kc)
+// 16-byte broadcasts.  No barrier.
+template <class T>
+__device__ __forceinline__ void cta_nmul_s(const T *M1, const T *v1, const T *M2, const T *v2, const T *base,
+                                           T *out, T sign, int n, int kc)
 {
+    using VT = typename Vec<T>::type;
+    constexpr int W = Vec<T>::W;
     const int tpc = (int)blockDim.x / n;
     const int r = threadIdx.x % n, jg = threadIdx.x / n;
     if (jg >= tpc) return;
     for (int j0 = jg; j0 < kc; j0 += 4 * tpc) {
-        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        T acc[4] = {T(0), T(0), T(0), T(0)};
         for (int mi = 0; mi < 2; ++mi) {
-            const float *M = mi == 0 ? M1 : M2;
-            const float *v = mi == 0 ? v1 : v2;
+            const T *M = mi == 0 ? M1 : M2;
+            const T *v = mi == 0 ? v1 : v2;
             if (!M) continue;
-            for (int c = 0; c < n; c += 4) {
-                const float m0 = M[r + (size_t)c * n], m1 = M[r + (size_t)(c + 1) * n];
-                const float m2 = M[r + (size_t)(c + 2) * n], m3 = M[r + (size_t)(c + 3) * n];
+            for (int c = 0; c < n; c += W) {
+                T mrow[W];
+#pragma unroll
+                for (int w = 0; w < W; ++w) mrow[w] = M[r + (size_t)(c + w) * n];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const int j = j0 + tpc * q;
                     if (j < kc) {
-                        const float4 x = *reinterpret_cast<const float4 *>(v + c + (size_t)j * n);
-                        acc[q] = fmaf(m0, x.x, fmaf(m1, x.y, fmaf(m2, x.z, fmaf(m3, x.w, acc[q]))));
+                        const VT x = *reinterpret_cast<const VT *>(v + c + (size_t)j * n);
+                        const T *xs = reinterpret_cast<const T *>(&x);
+#pragma unroll
+                        for (int w = 0; w < W; ++w) acc[q] = fma(mrow[w], xs[w], acc[q]);
                     }
                 }
             }
@@ -1466,7 +1472,7 @@ __device__ __forceinline__ void cta_nmul_s(const float *M1, const float *v1, con
             const int j = j0 + tpc * q;
             if (j < kc) {
                 const int o = r + j * n;
-                out[o] = (base ? base[o] : 0.0f) + sign * acc[q];
+                out[o] = (base ? base[o] : T(0)) + sign * acc[q];
             }
         }
     }
@@ -1481,9 +1487,9 @@ __device__ __forceinline__ void cta_nmul_s(const float *M1, const float *v1, con
 template <bool STAGED, class T>
 __device__ __forceinline__ void tmul(const T *M, const T *v, T *out, int n, int kc, T sign, bool accumulate)
 {
-    if constexpr (STAGED && std::is_same<T, float>::value) {
-        if (kc > 1 && (n & 3) == 0 && n <= (int)blockDim.x) {
-            cta_tmul_s(M, v, out, n, kc, sign, accumulate);
+    if constexpr (STAGED) {
+        if (kc > 1 && n % Vec<T>::W == 0 && n <= (int)blockDim.x) {
+            cta_tmul_s<T>(M, v, out, n, kc, sign, accumulate);
             return;
         }
     }
@@ -1500,11 +1506,9 @@ __device__ __forceinline__ void nmul(const T *M1, const T *v1, const T *M2, cons
                                      T sign, int n, int kc, T *red)
 {
     if constexpr (STAGED) {
-        if constexpr (std::is_same<T, float>::value) {
-            if (kc > 1 && (n & 3) == 0 && n * kc > (int)blockDim.x) {
-                cta_nmul_s(M1, v1, M2, v2, base, out, sign, n, kc);
-                return;
-            }
+        if (kc > 1 && n % Vec<T>::W == 0 && n * kc > (int)blockDim.x) {
+            cta_nmul_s<T>(M1, v1, M2, v2, base, out, sign, n, kc);
+            return;
         }
         cta_nmul<T>(M1, v1, M2, v2, base, out, sign, n, kc, red);
     } else {
