@@ -1,6 +1,7 @@
 """Benchmark: factorize! + solve! of one block-tridiagonal SPD system,
 N = 16384 blocks of n = 64, k = 1 right-hand side (
-A_i = G G^T + n I, B_i ~ N(0,1), d ~ U[0,1), seeded, generated on the GPU).
+A_i = G G^T + n I, B_i ~ N(0,1), d ~ U[0,1), generated once on the host by
+numpy's seeded Generator; both arms solve these same bytes).
 
 A "step" is one complete solve request: put d into the handle, factorize!,
 solve!, to a relative residual ||d - A x||_inf / (||A|| ||x|| + ||d||)
@@ -251,13 +252,22 @@ def time_leg(bss, A, B, d, T, precision, steps, warmup, restore_AB, ev_stream=No
     return total_ms / 1e3, fac, sol, data
 
 
-def run_k16(bss, A, B, dev, reps=3):
-    """Config 1 with k = 16 right-hand sides ~ U[0,1): factorize!+solve! in
-    mixed precision (to rel-resid 1e-12), plain FP64 and plain FP32."""
+def run_k16(bss, A, B, dev, peaks, hbm, check, reps=3):
+    """Config 1 with k = 16 right-hand sides ~ U[0,1) (numpy, seed 16):
+    factorize!+solve! in mixed precision (to rel-resid 1e-12), plain FP64 and
+    plain FP32; each result against the C oracle's FP64 x when `check`."""
+    import numpy as np
     import torch
     n, _, N = A.shape
-    g = torch.Generator(device=dev).manual_seed(16)
-    d16 = torch.rand((N, n, 16), device=dev, dtype=torch.float64, generator=g).permute(1, 2, 0)
+    rng = np.random.default_rng(16)
+    ds16 = np.ascontiguousarray(rng.random((N, 16, n)))  # storage order (N, k, n)
+    d16 = torch.from_numpy(ds16).to(dev).permute(2, 1, 0)
+    x_ref = None
+    if check:
+        As = A.permute(2, 1, 0).contiguous().cpu().numpy()
+        Bs = B.permute(2, 1, 0).contiguous().cpu().numpy()
+        x_ref = oracle_x(As, Bs, ds16)
+        del As, Bs
     out = {"workload": "N=16384, n=64, k=16, d~U[0,1)"}
     for name, T, prec in (("mixed", torch.float64, "mixed"), ("plain_fp64", torch.float64, "plain"),
                           ("plain_fp32", torch.float32, "plain")):
@@ -282,7 +292,13 @@ def run_k16(bss, A, B, dev, reps=3):
                 sol.append(e1.elapsed_time(e2))
         f, s_ = statistics.median(fac), statistics.median(sol)
         rr = rel_residual_dev(Ac.double(), Bc.double(), dt.double(), dc.double())
-        out[name] = {"solves_per_s": 1e3 / (f + s_), "factor_ms": f, "solve_ms": s_, "rel_residual": rr}
+        res = {"solves_per_s": 1e3 / (f + s_), "factor_ms": f, "solve_ms": s_, "rel_residual": rr,
+               "refine_steps": bss.get_info(data)["refine_steps"] if prec == "mixed" else 0}
+        if x_ref is not None:
+            res["rel_error_vs_oracle"] = rel_err_stor(dt.permute(2, 1, 0).double().cpu().numpy(), x_ref)
+        pk = ("f32", "FP32") if (prec == "mixed" or T == torch.float32) else ("f64", "FP64")
+        res["roofline"] = leg_roofline([(N, n, 16)], 4 if T == torch.float32 else 8, f, s_, peaks[pk[0]], pk[1], hbm)
+        out[name] = res
         del data, At, Bt, dt
         torch.cuda.empty_cache()
     return out
@@ -330,6 +346,73 @@ def hbm_peak():
         pass
     hbm = peaks.get("hbm_gbs")
     return (hbm, "measured") if hbm else (6800.0, "fallback")
+
+
+def fma_peaks():
+    """{"f64": TFLOP/s, "f32": TFLOP/s} of the FMA pipes of this GPU, measured
+    by the library's microbenchmark (bss_diag_fma_peak)."""
+    import ctypes
+    from blockstructuredsolvers_gb300 import _lib
+    L = _lib.load()
+    out = {}
+    for name, code in (("f64", _lib.BSS_F64), ("f32", _lib.BSS_F32)):
+        v = ctypes.c_double()
+        _lib.check(L.bss_diag_fma_peak(code, ctypes.byref(v)))
+        out[name] = v.value
+    return out
+
+
+def work(N, n, k):
+    """Algorithmic work of one factorize!+solve! from (N, n, k) alone:
+    F_factor = N n^3/3 + 2 (N-1) n^3 (potrf, trsm, syrk per block),
+    F_solve = k (2N + 4(N-1)) n^2, and the elements of A, B and d."""
+    F_fac = N * n ** 3 / 3.0 + 2.0 * (N - 1) * n ** 3
+    F_sol = k * (2.0 * N + 4.0 * (N - 1)) * n ** 2
+    elems_ab = (2 * N - 1) * n * n
+    return F_fac, F_sol, elems_ab, N * n * k
+
+
+def leg_roofline(systems, itemsize, factor_ms, solve_ms, peak_tflops, peak_name, hbm_gbs):
+    """GFLOP/s and the fraction of the roofline for a leg that solves the
+    (N, n, k) `systems` once in factor_ms + solve_ms: roofline time =
+    max(F / compute peak, bytes of A, B, d / HBM bandwidth), fraction =
+    roofline time / measured time.  Also the same for factorize! alone
+    (F_factor, bytes of A and B)."""
+    F_fac = F_sol = ab = dd = 0.0
+    for (N, n, k) in systems:
+        a, b, c, e = work(N, n, k)
+        F_fac, F_sol, ab, dd = F_fac + a, F_sol + b, ab + c, dd + e
+    t = (factor_ms + solve_ms) * 1e-3
+    t_flop = (F_fac + F_sol) / (peak_tflops * 1e12)
+    t_mem = itemsize * (ab + dd) / (hbm_gbs * 1e9)
+    roof = max(t_flop, t_mem)
+    f_flop = F_fac / (peak_tflops * 1e12)
+    f_mem = itemsize * ab / (hbm_gbs * 1e9)
+    return {"gflops": (F_fac + F_sol) / t / 1e9, "factor_gflops": F_fac / (factor_ms * 1e-3) / 1e9,
+            "roofline_ms": roof * 1e3, "roofline_frac": roof / t,
+            "factor_roofline_frac": max(f_flop, f_mem) / (factor_ms * 1e-3),
+            "bound": "compute" if t_flop >= t_mem else "hbm",
+            "peaks": f"{peak_name} FMA {peak_tflops:.2f} TFLOP/s (bss_diag_fma_peak, measured here); "
+                     f"HBM {hbm_gbs:.0f} GB/s",
+            "work": {"F_factor": F_fac, "F_solve": F_sol, "bytes": itemsize * (ab + dd)}}
+
+
+def oracle_x(As, Bs, ds, threads=None):
+    """x of the C oracle (backbone_cpu.jl restated, FP64) for storage-order
+    inputs; returns storage-order x (N, k, n).  Checker only."""
+    from oracle import cref
+    cref.lib(True)
+    cref.set_blas_threads(threads or os.cpu_count() or 1)
+    A, B, d = As.copy(), Bs.copy(), ds.copy()
+    assert cref.solve(A, B, d) == 0
+    return d
+
+
+def rel_err_stor(x, x_ref):
+    """max |x - x_ref| / max |x_ref| over storage-order arrays."""
+    import numpy as np
+    x = np.asarray(x, np.float64)
+    return float(np.abs(x - x_ref).max() / np.abs(x_ref).max())
 
 
 def time_sparse_cholesky(bss, A, B, d, hbm_gbs):
@@ -406,7 +489,14 @@ def run_ours(args):
     from blockstructuredsolvers_gb300 import _lib
     L = _lib.load()
 
-    A, B, d = gen_device(dev)
+    # the same seeded host inputs as the reference arm, in Julia storage order
+    As, Bs, ds = gen_host()
+    # column-major (n, n, N) device views, the handle tensors' layout
+    A = torch.from_numpy(As).to(dev).permute(2, 1, 0)
+    B = torch.from_numpy(Bs).to(dev).permute(2, 1, 0)
+    d = torch.from_numpy(ds).to(dev).permute(2, 1, 0)
+    hbm, peak_kind = hbm_peak()
+    peaks = fma_peaks()
     # ---- headline: mixed precision, inputs resident in HBM -------------------
     sampler = ClockSampler(local)
     if world > 1:
@@ -421,32 +511,47 @@ def run_ours(args):
     x = data.d_tensor[:, :, :N_BLK]
     relres = rel_residual_dev(A, B, x, d)
     x_head = x.permute(2, 1, 0).contiguous().cpu().numpy()  # (N, k, n): the oracle's storage order
-    launches_per_step = None
+    del data, x
     # the warmup steps launched too: count per step from the total
     launches_per_step = launches / max(args.steps + args.warmup, 1)
     from blockstructuredsolvers_gb300 import replicas
     secs = replicas.reduce_max(secs)  # the slowest replica's time
     value = world * args.steps / secs
+    x_ref = oracle_x(As, Bs, ds) if rank == 0 else None
+    err_head = rel_err_stor(x_head, x_ref) if rank == 0 else None
+    cfg1 = [(N_BLK, N_SZ, K_RHS)]
+    head_roof = leg_roofline(cfg1, 8, statistics.median(fac), statistics.median(sol), peaks["f32"], "FP32", hbm)
 
-    extra = {}
+    extra = {"peaks_measured": {"fp64_fma_tflops": peaks["f64"], "fp32_fma_tflops": peaks["f32"],
+                                "hbm_gbs": hbm, "hbm_source": f"MEASURED_PEAKS.json ({peak_kind})"}}
     if not args.quick:
         # ---- plain FP64 and plain FP32 GPU paths (same request) ---------------
-        s64, f64, so64, d64 = time_leg(bss, A, B, d, torch.float64, "plain", max(3, args.steps // 4), 1, True)
+        n64 = max(3, args.steps // 4)
+        s64, f64, so64, d64 = time_leg(bss, A, B, d, torch.float64, "plain", n64, 1, True)
         rr64 = rel_residual_dev(A, B, d64.d_tensor[:, :, :N_BLK], d)
+        x64 = d64.d_tensor[:, :, :N_BLK].permute(2, 1, 0).contiguous().cpu().numpy()
         del d64
-        s32, f32, so32, d32 = time_leg(bss, A, B, d, torch.float32, "plain", max(3, args.steps // 4), 1, True)
+        s32, f32, so32, d32 = time_leg(bss, A, B, d, torch.float32, "plain", n64, 1, True)
         rr32 = rel_residual_dev(A.float().double(), B.float().double(), d32.d_tensor[:, :, :N_BLK].double(),
                                 d.float().double())
+        x32 = d32.d_tensor[:, :, :N_BLK].permute(2, 1, 0).double().contiguous().cpu().numpy()
         del d32
-        n64 = max(3, args.steps // 4)
         extra["reference_algorithm_gpu"] = time_reference_algorithm(bss, A, B, d)
-        extra["sparse_cholesky_gpu"] = time_sparse_cholesky(bss, A, B, d, hbm_peak()[0])
-        extra["k16"] = run_k16(bss, A, B, dev)
-        extra["plain_fp64"] = {"solves_per_s": n64 / s64, "factor_ms": statistics.median(f64),
-                               "solve_ms": statistics.median(so64), "rel_residual": rr64,
-                               "note": "includes the device copy of A, B, d into the handle per step"}
-        extra["plain_fp32"] = {"solves_per_s": n64 / s32, "factor_ms": statistics.median(f32),
-                               "solve_ms": statistics.median(so32), "rel_residual_fp32_system": rr32,
+        extra["sparse_cholesky_gpu"] = time_sparse_cholesky(bss, A, B, d, hbm)
+        extra["k16"] = run_k16(bss, A, B, dev, peaks, hbm, rank == 0)
+        fm64, sm64 = statistics.median(f64), statistics.median(so64)
+        extra["plain_fp64"] = {"solves_per_s": n64 / s64, "factor_ms": fm64, "solve_ms": sm64,
+                               "rel_residual": rr64,
+                               "rel_error_vs_oracle": rel_err_stor(x64, x_ref) if rank == 0 else None,
+                               "refine_steps": 0,
+                               "roofline": leg_roofline(cfg1, 8, fm64, sm64, peaks["f64"], "FP64", hbm),
+                               "note": "solves/s includes the device copy of A, B, d into the handle per step"}
+        fm32, sm32 = statistics.median(f32), statistics.median(so32)
+        extra["plain_fp32"] = {"solves_per_s": n64 / s32, "factor_ms": fm32, "solve_ms": sm32,
+                               "rel_residual_fp32_system": rr32,
+                               "rel_error_vs_oracle": rel_err_stor(x32, x_ref) if rank == 0 else None,
+                               "refine_steps": 0,
+                               "roofline": leg_roofline(cfg1, 4, fm32, sm32, peaks["f32"], "FP32", hbm),
                                "note": "FP32 accuracy only; not a rel-resid <= 1e-12 result"}
 
     # ---- e2e through the public API with host buffers ----------------------
@@ -459,9 +564,9 @@ def run_ours(args):
     e2e = None
     if not args.quick:
         # host copies in the handle's storage order: (N, c, r) C-order == column-major blocks
-        Ah = A.permute(2, 1, 0).contiguous().cpu().pin_memory()
-        Bh = B.permute(2, 1, 0).contiguous().cpu().pin_memory()
-        dh = d.permute(2, 1, 0).contiguous().cpu().pin_memory()
+        Ah = torch.from_numpy(As).pin_memory()
+        Bh = torch.from_numpy(Bs).pin_memory()
+        dh = torch.from_numpy(ds).pin_memory()
         streams = [torch.cuda.Stream(), torch.cuda.Stream()]
         slots = []
         for st in streams:
@@ -470,7 +575,7 @@ def run_ours(args):
             slots.append((st, data, data.A_tensor[:, :, :N_BLK].permute(2, 1, 0),
                           data.B_tensor[:, :, :N_BLK - 1].permute(2, 1, 0),
                           data.d_tensor[:, :, :N_BLK].permute(2, 1, 0), torch.empty_like(dh).pin_memory()))
-        ne = max(4, args.steps // 4)
+        ne = max(20, args.steps // 4)
 
         def e2e_step(slot):
             st, data, At, Bt, dt, xh = slot
@@ -491,42 +596,37 @@ def run_ours(args):
             e2e_step(slots[i % 2])
         torch.cuda.synchronize()
         te = time.perf_counter() - tt0
+        n1 = max(5, ne // 2)
         tt0 = time.perf_counter()
-        for i in range(max(3, ne // 2)):
+        for i in range(n1):
             e2e_step(slots[0])
         torch.cuda.synchronize()
-        te1 = (time.perf_counter() - tt0) / max(3, ne // 2)
+        te1 = (time.perf_counter() - tt0) / n1
         x_e2e = slots[0][5].permute(2, 1, 0)  # (n, k, N) view of the last x
         rr_e2e = rel_residual_dev(A, B, x_e2e.to(dev), d)
         bi = (Ah.numel() + Bh.numel() + dh.numel()) * 8
         bo = slots[0][5].numel() * 8
         e2e = {"value": world * ne / te, "unit": "solves/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
+               "requests_timed": ne,
                "mode": "two handles on two streams, alternate requests, copies inside the timed region",
-               "serial_one_handle": world / te1, "rel_residual_last_x": rr_e2e}
+               "serial_one_handle": world / te1, "rel_residual_last_x": rr_e2e,
+               "rel_error_vs_oracle_last_x": rel_err_stor(slots[0][5].numpy(), x_ref) if rank == 0 else None}
         del slots
 
     # ---- roofline of the dominant kernel ----------------------------------
-    hbm, peak_kind = hbm_peak()
     roof = roofline_chain_factor(bss, A, B, d, hbm, peak_kind)
 
     cpu_base = None
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         try:
-            As = A.permute(2, 1, 0).contiguous().cpu().numpy()
-            Bs = B.permute(2, 1, 0).contiguous().cpu().numpy()
-            ds = d.permute(2, 1, 0).contiguous().cpu().numpy()
-            from oracle import cref
             cores = os.cpu_count() or 1
             t1, _ = cpu_solve_time(As, Bs, ds, reps=1, threads=1)
             tN, xcpu = cpu_solve_time(As, Bs, ds, reps=1, threads=cores)
             best = min((t1, 1), (tN, cores))
-            import numpy as np
-            err = float(np.abs(x_head - xcpu).max() / np.abs(xcpu).max())
             cpu_base = {"value": 1.0 / best[0], "unit": "solves/s", "cores": best[1], "kind": "port",
                         "sample": "one full factorize!+solve! of the workload (C restatement of "
                                   "backbone_cpu.jl on OpenBLAS); best of 1 thread and "
-                                  f"{cores} BLAS threads",
-                        "headline_x_rel_error_vs_oracle": err}
+                                  f"{cores} BLAS threads"}
         except Exception as e:  # pragma: no cover
             cpu_base = {"value": None, "unit": "solves/s", "cores": None, "kind": "port", "sample": f"failed: {e}"}
 
@@ -534,22 +634,24 @@ def run_ours(args):
     if not args.quick and not args.no_extra:
         del A, B, d
         torch.cuda.empty_cache()
-        others["large_system_n128"] = run_large_system(bss, dev)
-        others["uneven_batch"] = run_uneven_batch(bss, dev)
-        others["served_kalman"] = run_served_legs(bss)
+        others["large_system_n128"] = run_large_system(bss, dev, peaks, hbm, rank == 0)
+        others["uneven_batch"] = run_uneven_batch(bss, dev, peaks, hbm, rank == 0)
+        others["served_kalman"] = run_served_legs(bss, rank == 0)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 factor + f64 refinement",
-            "data": "synthetic (seeded torch generator on device: A_i = G G^T + n I, B_i ~ N(0,1), d ~ U[0,1))",
+            "data": "synthetic (seeded numpy on the host, the reference arm's bytes: "
+                    "A_i = G G^T + n I, B_i ~ N(0,1), d ~ U[0,1))",
             "config": {"workload": WORKLOAD, "N": N_BLK, "n": N_SZ, "k": K_RHS, "precision": "mixed",
                        "levels": info["levels"], "coarsest_blocks": info["coarsest_blocks"],
                        "l2": "inputs (1.07 GB FP64 A,B) larger than L2; no flush",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "factor_ms_median": statistics.median(fac), "solve_ms_median": statistics.median(sol),
-            "refine_steps": info["refine_steps"], "rel_residual": relres,
+            "refine_steps": info["refine_steps"], "rel_residual": relres, "rel_error_vs_oracle": err_head,
+            "gflops": head_roof["gflops"], "roofline_8d": head_roof,
             "gpu_launches": int(round(launches_per_step * args.steps)),
             "gpu_launches_per_step": launches_per_step,
             "clocks": clocks, "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e,
@@ -643,10 +745,40 @@ def gen_kf_stream(n_requests, rate, repeat_frac=0.3, seed=4, recent=32):
     return models, reqs
 
 
-def run_served(bss, precision, models, reqs, budget=100 * 10**9, streams=8):
+def served_sample_check(models, reqs, ids, every=40):
+    """Every `every`-th completed request of a served stream against the C
+    oracle: its blocks rebuilt on the host by the oracle's restatement of
+    build_kf_blocks, solved in FP64 on the host cores; returns the worst
+    relative error of x and the worst FP64 relative residual over the
+    sample, and the sample size."""
+    import numpy as np
+    import oracle.oracle as O
+    from oracle import cref
+    cref.lib(True)
+    cref.set_blas_threads(1)
+    worst_err = worst_res = 0.0
+    cnt = 0
+    for i in range(0, len(reqs), every):
+        if ids[i] is None:
+            continue
+        r = reqs[i]
+        mdl = models[r["model"]]
+        n, m = mdl["n"], mdl["n"] // 2
+        Y = np.swapaxes(r["y"].numpy(), 1, 2)  # (N, m, k) math
+        A, B, d = O.kf_blocks(mdl["F"], mdl["H"], 10.0 * np.eye(n), 2.0 * np.eye(m), Y)
+        x_ref = cref.solve_math(A, B, d, np.float64)
+        x = np.swapaxes(r["x"].numpy(), 1, 2)
+        worst_err = max(worst_err, O.rel_error(x, x_ref))
+        worst_res = max(worst_res, O.rel_residual(A, B, x, d))
+        cnt += 1
+    return worst_err, worst_res, cnt
+
+
+def run_served(bss, precision, models, reqs, budget=100 * 10**9, streams=8, check=False):
     """Replay the stream against a server: a submitter thread releases each
     request at its arrival time; returns solves/s, latency percentiles and
-    the worst relative residual the solver reported."""
+    the worst relative residual the solver reported (mixed precision), and
+    with `check` a sample of the results against the C oracle."""
     import threading
     srv = bss.Server(hbm_budget_bytes=budget, streams=streams, max_inflight=64, precision=precision)
     fids = {}
@@ -687,11 +819,17 @@ def run_served(bss, precision, models, reqs, budget=100 * 10**9, streams=8):
         steps.append(info["refine_steps"])
     st = srv.stats()
     srv.close()
-    return {"solves_per_s": st["completed"] / st["busy_s"] if st["busy_s"] > 0 else None,
-            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
-            "completed": st["completed"], "failed": failed + len(errors), "evictions": st["evictions"],
-            "bytes_peak": st["bytes_peak"], "worst_rel_residual": worst if precision == "mixed" else None,
-            "mean_refine_steps": (sum(steps) / len(steps)) if steps else None}
+    out = {"solves_per_s": st["completed"] / st["busy_s"] if st["busy_s"] > 0 else None,
+           "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
+           "completed": st["completed"], "failed": failed + len(errors), "evictions": st["evictions"],
+           "bytes_peak": st["bytes_peak"], "worst_rel_residual": worst if precision == "mixed" else None,
+           "mean_refine_steps": (sum(steps) / len(steps)) if steps else None,
+           "max_refine_steps": max(steps) if steps else None}
+    if check:
+        e, r, c = served_sample_check(models, reqs, ids)
+        out.update({"sample_worst_rel_error_vs_oracle": e, "sample_worst_rel_residual": r,
+                    "sample": f"{c} requests (every 40th), blocks rebuilt on the host, C oracle FP64"})
+    return out
 
 
 # --------------------------------------------------------------------------
@@ -758,29 +896,53 @@ def _timed_handle_leg(bss, A, B, d, precision, reps):
             sol.append(e1.elapsed_time(e2))
     info = bss.get_info(data)
     relres = rel_residual_dev(A, B, dt, d)
+    x = dt.permute(2, 1, 0).contiguous().cpu().numpy()
     del data
     torch.cuda.empty_cache()
     f, s_ = statistics.median(fac), statistics.median(sol)
     return {"solves_per_s": 1e3 / (f + s_), "factor_ms": f, "solve_ms": s_, "rel_residual": relres,
-            "refine_steps": info["refine_steps"], "levels": info["levels"]}
+            "refine_steps": info["refine_steps"], "levels": info["levels"]}, x
 
 
-def run_large_system(bss, dev):
+def run_large_system(bss, dev, peaks, hbm, check):
+    """N=65536 blocks of n=128, k=4 (log-spaced spectra over [1, 1e4]):
+    mixed precision and plain FP64 on the device; each x against the C
+    oracle's FP64 solve of the same inputs on the host cores."""
     import torch
     A, B, d = gen_logspectrum(dev)
-    out = {"workload": "N=65536, n=128, k=4, A_i=Q diag(logspace(0,4)) Q^T, B_i=0.45 U V^T, d~N(0,1)",
-           "mixed": _timed_handle_leg(bss, A, B, d, "mixed", 3),
-           "plain_fp64": _timed_handle_leg(bss, A, B, d, "plain", 1)}
+    n, _, N = A.shape
+    k = d.shape[1]
+    out = {"workload": "N=65536, n=128, k=4, A_i=Q diag(logspace(0,4)) Q^T, B_i=0.45 U V^T, d~N(0,1)"}
+    legs = {}
+    for name, prec, reps in (("mixed", "mixed", 3), ("plain_fp64", "plain", 1)):
+        res, x = _timed_handle_leg(bss, A, B, d, prec, reps)
+        pk = ("f32", "FP32") if prec == "mixed" else ("f64", "FP64")
+        res["roofline"] = leg_roofline([(N, n, k)], 8, res["factor_ms"], res["solve_ms"], peaks[pk[0]], pk[1], hbm)
+        out[name] = res
+        legs[name] = x
     out["mixed_over_plain_fp64"] = out["mixed"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
-    del A, B, d
+    if check:
+        As = A.permute(2, 1, 0).contiguous().cpu().numpy()
+        Bs = B.permute(2, 1, 0).contiguous().cpu().numpy()
+        ds = d.permute(2, 1, 0).contiguous().cpu().numpy()
+        t0 = time.perf_counter()
+        x_ref = oracle_x(As, Bs, ds)
+        out["oracle_s"] = time.perf_counter() - t0
+        del As, Bs, ds
+        for name, x in legs.items():
+            out[name]["rel_error_vs_oracle"] = rel_err_stor(x, x_ref)
+    del A, B, d, legs
     torch.cuda.empty_cache()
     return out
 
 
-def run_uneven_batch(bss, dev, steps=3, seed=3):
+def run_uneven_batch(bss, dev, peaks, hbm, check, steps=3, seed=3, sample_every=32):
     """2048 independent systems, N ~ U{16..1024}, n from {16,32,48,64,96,128},
     k ~ U{1..8}, A_i = G G^T + 2n I, B_i ~ 0.5 N(0,1), d ~ U[0,1); mixed
-    precision, one batch (graph-replayed after the first call)."""
+    precision, one batch (graph-replayed after the first call).  Every
+    `sample_every`-th system is also solved by the C oracle on the host cores
+    (one thread per system, all cores: the CPU baseline of this config) and
+    its GPU x compared with the oracle's."""
     import numpy as np
     import torch
     rng = np.random.default_rng(seed)
@@ -802,6 +964,9 @@ def run_uneven_batch(bss, dev, steps=3, seed=3):
                 sv.B_tensor.copy_(Bm.permute(1, 2, 0))
             sv.d_tensor.copy_(torch.rand((N, n, k), dtype=torch.float64, device=dev, generator=g).permute(1, 2, 0))
 
+    sample = list(range(0, S, sample_every))
+    host = {}
+
     def leg(prec):  # in its own scope: the batch dies with the function's locals
         b = bss.initialize_multi(Ns.tolist(), ns.tolist(), ks.tolist(), torch.float64, precision=prec)
         fac, sol = [], []
@@ -810,6 +975,11 @@ def run_uneven_batch(bss, dev, steps=3, seed=3):
         for r in range(nsteps + 1):
             if prec == "plain" or dsave is None:  # plain factors in place: fresh inputs every rep
                 fill(b)
+                if check and not host:  # the sampled systems' inputs, storage order
+                    for i in sample:
+                        sv = b.systems[i]
+                        host[i] = tuple(t.permute(2, 1, 0).contiguous().cpu().numpy()
+                                        for t in (sv.A_tensor, sv.B_tensor, sv.d_tensor))
                 if prec == "mixed":
                     dsave = [sv.d_tensor.clone() for sv in b.systems]
             else:
@@ -832,26 +1002,58 @@ def run_uneven_batch(bss, dev, steps=3, seed=3):
         if prec == "mixed":
             out["worst_rel_residual"] = max(b.info(i)["rel_residual"] for i in range(S))
             out["max_refine_steps"] = max(b.info(i)["refine_steps"] for i in range(S))
-        return out
+        else:
+            out["max_refine_steps"] = 0
+        pk = ("f32", "FP32") if prec == "mixed" else ("f64", "FP64")
+        out["roofline"] = leg_roofline(list(zip(Ns.tolist(), ns.tolist(), ks.tolist())), 8, f, s_,
+                                       peaks[pk[0]], pk[1], hbm)
+        xs = {}
+        if check:
+            import oracle.oracle as O
+            xs = {i: b.systems[i].d_tensor.permute(2, 1, 0).contiguous().cpu().numpy() for i in sample}
+            out["sample_worst_rel_residual"] = max(
+                O.rel_residual(O.from_storage(host[i][0]), O.from_storage(host[i][1]), O.from_storage(xs[i]),
+                               O.from_storage(host[i][2])) for i in sample)
+        return out, xs
 
     import gc
+    xs_by = {}
     for prec in ("mixed", "plain"):
-        res["mixed" if prec == "mixed" else "plain_fp64"] = leg(prec)
+        name = "mixed" if prec == "mixed" else "plain_fp64"
+        res[name], xs_by[name] = leg(prec)
         gc.collect()
         torch.cuda.empty_cache()
+    if check:
+        # the sampled systems on the host cores: one BLAS thread per system, all cores
+        from oracle import cref
+        cores = os.cpu_count() or 1
+        cref.lib(True)
+        cref.set_blas_threads(1)
+        systems = [tuple(a.copy() for a in host[i]) for i in sample]
+        t0 = time.perf_counter()
+        info = cref.solve_many(systems, cores)
+        tcpu = time.perf_counter() - t0
+        assert not info.any()
+        xref = {i: sy[2] for i, sy in zip(sample, systems)}
+        res["cpu_baseline"] = {"value": len(sample) / tcpu, "unit": "systems/s", "cores": cores, "kind": "port",
+                               "sample": f"{len(sample)} of the {S} systems (every {sample_every}th), "
+                                         "C restatement of backbone_cpu.jl, one BLAS thread per system, "
+                                         f"{cores} systems at a time"}
+        for name, xs in xs_by.items():
+            res[name]["sample_worst_rel_error_vs_oracle"] = max(rel_err_stor(xs[i], xref[i]) for i in sample)
     res["mixed_over_plain_fp64"] = res["mixed"]["systems_per_s"] / res["plain_fp64"]["systems_per_s"]
     return res
 
 
-def run_served_legs(bss, n_requests=1200, rate=2000.0):
+def run_served_legs(bss, check, n_requests=1200, rate=2000.0):
     models, reqs = gen_kf_stream(n_requests, rate)
     out = {"workload": f"{n_requests} Kalman-smoother requests, n in {{8,16,32,64}}, N~U{{50..5000}}, "
                        f"Poisson {rate:g} req/s, 30% repeat RHS on resident factors, 100 GB budget"}
-    out["mixed"] = run_served(bss, "mixed", models, reqs)
-    out["plain_fp64"] = run_served(bss, "plain", models, reqs)
+    out["mixed"] = run_served(bss, "mixed", models, reqs, check=check)
+    out["plain_fp64"] = run_served(bss, "plain", models, reqs, check=check)
     sat = [dict(r, t=0.0) for r in reqs]
-    out["saturated_mixed"] = run_served(bss, "mixed", models, sat)
-    out["saturated_plain_fp64"] = run_served(bss, "plain", models, sat)
+    out["saturated_mixed"] = run_served(bss, "mixed", models, sat, check=check)
+    out["saturated_plain_fp64"] = run_served(bss, "plain", models, sat, check=check)
     out["saturated_mixed_over_plain_fp64"] = (out["saturated_mixed"]["solves_per_s"] /
                                               out["saturated_plain_fp64"]["solves_per_s"])
     return out
@@ -890,18 +1092,54 @@ def roofline_chain_factor(bss, A, B, d, hbm_gbs, peak_kind):
     alg_bytes = interior * (2 * nn * 8 + 3 * nn * 4) + (Q.value + 1) * nn * 8
     ms = statistics.median(ts)
     ach = alg_bytes / (ms * 1e-3) / 1e9
-    # DRAM bytes (read + write) of this kernel from one ncu capture of the same
-    # launch at N=4096 (profiles/chain_factor_mixed_N4096_n64.md: 262.0 + 156.6 MB
-    # over 3791 interior blocks), scaled by interior blocks: the traffic of a
-    # chain grows in proportion to its blocks
-    traffic = (261.9712e6 + 156.595968e6) / 3791 * interior
-    return {"kernel": "chain_factor_kernel<double,float,64> (level 0) + assemble_schur", "bound": "hbm",
+    # DRAM bytes (read + write) per interior block of this kernel from one ncu
+    # capture of a smaller launch (the traffic of a chain grows in proportion
+    # to its blocks), used only while the kernel source still matches the
+    # capture's
+    per_blk, src = captured_traffic()
+    traffic = per_blk * interior if per_blk else None
+    return {"kernel": "chain_factor level 0 (FP64 A, B in; FP32 V, W, Y out) + assemble_schur", "bound": "hbm",
             "achieved": ach, "peak": hbm_gbs, "unit": "GB/s", "frac": ach / hbm_gbs,
             "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})", "duration_ms": ms,
             "algorithmic_bytes": alg_bytes, "partitions": Q.value, "traffic": traffic,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the N=4096 capture, "
-                              "scaled by interior blocks",
-            "note": "latency/FMA-bound chain: the HBM fraction is low by construction"}
+            "traffic_source": src,
+            "note": "latency-bound chain: the HBM fraction is low by construction"}
+
+
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "chain_factor_mixed_N4096_n64.md")
+KERNEL_SOURCES = [os.path.join(ROOT, "blockstructuredsolvers_gb300", "csrc", f)
+                  for f in ("bss_kernels.cuh", "bss_tc.cuh", "bss_chain64_tc.cuh")]
+
+
+def kernel_source_sha16():
+    """sha256 (first 16 hex digits) of the device sources of the chain kernels."""
+    import hashlib
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        if os.path.exists(f):
+            with open(f, "rb") as fh:
+                h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def captured_traffic():
+    """(bytes per interior block, source note) from the ncu summary of the
+    level-0 chain factor kernel, or (None, why) when its recorded kernel
+    source hash differs from the current sources."""
+    import re
+    try:
+        with open(TRAFFIC_PROFILE) as f:
+            txt = f.read()
+    except OSError:
+        return None, "no ncu summary"
+    m1 = re.search(r"traffic_per_interior_block_bytes\s*=\s*([0-9.eE+]+)", txt)
+    m2 = re.search(r"kernel_source_sha16\s*=\s*([0-9a-f]{16})", txt)
+    if not (m1 and m2):
+        return None, "the ncu summary records no per-block traffic"
+    if m2.group(1) != kernel_source_sha16():
+        return None, "the ncu summary was taken on other kernel sources (hash differs): traffic not reported"
+    return float(m1.group(1)), ("ncu dram__bytes_read.sum + dram__bytes_write.sum per interior block of the "
+                                "capture in " + os.path.basename(TRAFFIC_PROFILE) + ", times interior blocks")
 
 
 def run_case(name, reps=3):

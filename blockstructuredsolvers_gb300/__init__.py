@@ -138,7 +138,7 @@ def _stream_ptr(stream):
 def initialize_batched(N: int, n: int, T=None, M=None, *, k: int = 1, precision: str = "plain",
                        plan: str = "auto", max_refine: int = 10, tol: float = 1e-12,
                        target_partitions: int = 0, seq_cutoff: int = 0, use_graphs: bool = True,
-                       stream=None) -> BlockTriDiagData_batched:
+                       coarsest_fp64: bool = False, stream=None) -> BlockTriDiagData_batched:
     """initialize_batched(N, n, T, CuArray) (src/gpu_batched.jl:165-182).
 
     ``M`` is accepted for signature parity (the reference passes CuArray) and
@@ -147,6 +147,8 @@ def initialize_batched(N: int, n: int, T=None, M=None, *, k: int = 1, precision:
     reference planner's level sequence; "auto" sizes partitions to the GPU.
     ``use_graphs``: after the first call, factorize!/solve! replay CUDA graphs
     (the mixed solve's refinement loop runs on the device).
+    ``coarsest_fp64`` (mixed only): factor and solve the sequential coarsest
+    Schur complement in FP64 instead of FP32.
     """
     torch = _torch()
     code, tdt = _dtype_code(torch.float64 if T is None else T)
@@ -158,6 +160,7 @@ def initialize_batched(N: int, n: int, T=None, M=None, *, k: int = 1, precision:
     o.target_partitions = int(target_partitions)
     o.seq_cutoff = int(seq_cutoff)
     o.use_graphs = 1 if use_graphs else 0
+    o.coarsest_fp64 = 1 if coarsest_fp64 else 0
     L = _lib.load()
     h = ctypes.c_void_p()
     torch.cuda.current_device()  # make torch bind the device's primary context first

@@ -54,6 +54,7 @@ extern "C" void bss_default_options(bss_options *o)
     o->use_graphs = 1;
     o->tol = 1e-12;
     o->chain_blocks = 0;
+    o->coarsest_fp64 = 0;
 }
 
 extern "C" const char *bss_last_error_string(void) { return g_last_error.c_str(); }
@@ -227,13 +228,15 @@ int bss::plan_handle(bss_handle *h)
     }
     {
         // the sequential coarsest level: plain in the tensor dtype; mixed in
-        // FP32 like every other level (the FP64 refinement corrects the whole
-        // factorization, and GB300's FP64 pipe runs at ~1/64 of FP32)
+        // FP32 like every other level by default (the FP64 refinement corrects
+        // the whole factorization, and GB300's FP64 pipe runs at ~1/64 of
+        // FP32), or in FP64 on request (the coarsest Schur complement is the
+        // worst-conditioned block system of the recursion)
         Level L;
         L.N = coarsest;
         L.Q = 0;
         L.seq = true;
-        L.t = mixed ? F32 : D;
+        L.t = mixed ? (h->opt.coarsest_fp64 ? F64 : F32) : D;
         L.tin = h->levels.empty() ? D : L.t;
         h->levels.push_back(L);
     }

@@ -803,6 +803,7 @@ extern "C" int bss_batch_create(int32_t nsys, const int64_t *N, const int64_t *n
         // cheapest schedule; the batch supplies the parallelism).
         const long long chain = batch_chain_blocks(b->opt, (int)n[s], dtype);
         h->opt.plan = BSS_PLAN_AUTO;
+        h->opt.coarsest_fp64 = 0;  // the batch's coarsest chains run in the factor dtype
         h->opt.target_partitions = (int)std::max<long long>(1, N[s] / chain);
         if (N[s] < 2 * chain) h->opt.seq_cutoff = (int)std::max<long long>(1, N[s]);
         rc = plan_handle(h);

@@ -180,3 +180,72 @@ extern "C" int bss_diag_wait_timeout(int64_t polls, int64_t *timed_out, int64_t 
     *cycles = h[1];
     return BSS_OK;
 }
+
+// ---------------------------------------------------------------------------
+// FMA-pipe peak microbenchmark: every thread runs 8 independent FMA chains
+// (enough to cover the pipe latency with 8 warps per scheduler) for `iters`
+// iterations; one FMA = 2 flops.  The result is written only when the
+// impossible flag is set, which keeps the compiler from removing the chains.
+// ---------------------------------------------------------------------------
+namespace {
+template <class T>
+__global__ void __launch_bounds__(256) fma_peak_kernel(T a, T b, int iters, int flag, T *out)
+{
+    T x0 = (T)threadIdx.x, x1 = x0 + T(1), x2 = x0 + T(2), x3 = x0 + T(3);
+    T x4 = x0 + T(4), x5 = x0 + T(5), x6 = x0 + T(6), x7 = x0 + T(7);
+#pragma unroll 4
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, b);
+        x1 = fma(x1, a, b);
+        x2 = fma(x2, a, b);
+        x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b);
+        x5 = fma(x5, a, b);
+        x6 = fma(x6, a, b);
+        x7 = fma(x7, a, b);
+    }
+    if (flag) out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+template <class T>
+int fma_peak(double *tflops)
+{
+    int dev = 0, sms = 0;
+    BSS_CUDA(cudaGetDevice(&dev));
+    BSS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 8, threads = 256;  // 8 CTAs of 256 threads per SM: 64 warps
+    const int iters = sizeof(T) == 8 ? 1 << 12 : 1 << 16;
+    cudaEvent_t e0, e1;
+    BSS_CUDA(cudaEventCreate(&e0));
+    BSS_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int r = 0; r < 4; ++r) {  // first launch warms up; best of the rest
+        cudaEventRecord(e0, 0);
+        fma_peak_kernel<T><<<blocks, threads>>>(T(0.999), T(1e-3), iters, 0, (T *)nullptr);
+        count_launch();
+        cudaEventRecord(e1, 0);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return cuda_fail(e, "fma_peak_kernel");
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r > 0) best = std::min(best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const double flops = 2.0 * 8.0 * (double)iters * (double)blocks * (double)threads;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    return BSS_OK;
+}
+}  // namespace
+
+extern "C" int bss_diag_fma_peak(int32_t dtype, double *tflops)
+{
+    if (!tflops) return fail(BSS_ERR_ARG, "bss_diag_fma_peak: tflops is NULL");
+    if (dtype == BSS_F64) return fma_peak<double>(tflops);
+    if (dtype == BSS_F32) return fma_peak<float>(tflops);
+    return fail(BSS_ERR_ARG, "bss_diag_fma_peak: dtype must be BSS_F32 or BSS_F64");
+}

@@ -207,10 +207,17 @@ int run(long long N, int n, int k, T *A, T *B, T *d, cudaStream_t s)
             NA_CHECK((launch_chain_bwd<T, T>(a, s)));
         }
     }
-    unsigned long long key = 0;
-    NA_CHECK(cudaMemcpyAsync(&key, &st->bad_key, sizeof(key), cudaMemcpyDeviceToHost, s));
+    // one copy of the whole status: the failed-pivot key and the flag the
+    // tensor-core kernels set when a bounded wait expired
+    DevStatus hs;
+    NA_CHECK(cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s));
     NA_CHECK(cudaStreamSynchronize(s));
 #undef NA_CHECK
+    if (hs.tc_timeout) {
+        g_noalloc_err = "a bounded tensor-core wait expired during factorize; the factors are void";
+        return BSS_ERR_TIMEOUT;
+    }
+    const unsigned long long key = hs.bad_key;
     if (key != ~0ULL) {
         g_noalloc_err = "pivot failed at level " + std::to_string(key >> 40) + ", block " +
                         std::to_string(key & ((1ULL << 40) - 1));
@@ -228,7 +235,14 @@ extern "C" int bss_factor_solve_noalloc(int64_t N, int64_t n, int64_t k, int32_t
         set_last_error("bss_factor_solve_noalloc: bad argument");
         return BSS_ERR_ARG;
     }
-    if (tile_for((int)n) == 0) {
+    // range checks before the narrowing casts below: block indices are
+    // reported in 40 bits, n and k are int in the kernels
+    if (N >= (1LL << 40) || k > 0x7FFFFFFFLL) {
+        set_last_error("bss_factor_solve_noalloc: N=" + std::to_string(N) + " or k=" + std::to_string(k) +
+                       " out of range");
+        return BSS_ERR_ARG;
+    }
+    if (n > MAX_WIDE_N || tile_for((int)n) == 0) {
         set_last_error("bss_factor_solve_noalloc: block size n=" + std::to_string(n) + " is not supported");
         return BSS_ERR_UNSUPPORTED;
     }

@@ -2,8 +2,8 @@
  * bss.h -- C ABI of the GB300 (sm_103a) batched block-tridiagonal SPD solver.
  *
  * Drop-in for BlockStructuredSolvers.jl's batched GPU solver.  A Julia caller
- * binds these entry points with `ccall`; Python binds
- * them with ctypes (blockstructuredsolvers_gb300/_lib.py).  No torch or CUDA
+ * binds these entry points with `ccall`; Python binds them with ctypes
+ * (blockstructuredsolvers_gb300/_lib.py).  No torch or CUDA
  * C++ types appear in the signatures: streams are passed as `void*`
  * (a cudaStream_t), device buffers as `void*`.
  *
@@ -62,6 +62,10 @@ typedef struct {
                                   every system (0 = auto per n and precision); a
                                   system's plan depends only on its own N, n and
                                   this value, never on the other systems        */
+    int32_t coarsest_fp64;     /* mixed, single-system handles: factor and solve the
+                                  sequential coarsest level in FP64 (0 = FP32, the
+                                  default; the FP64 refinement corrects the whole
+                                  factorization either way).  Batches ignore it. */
 } bss_options;
 
 typedef struct {
@@ -169,12 +173,16 @@ int bss_get_level(bss_handle *h, int32_t level, int64_t *N, int64_t *Q, void **A
  * loading this library reserves until the process exits; this call performs
  * no cudaMalloc/cudaFree and calls no allocating library routine.  A problem
  * whose workspace does not fit is rejected with BSS_ERR_ARG before any work
- * is launched.  The first call on a device looks up the array's device
- * address with that device current; make that first call before any stream
- * capture.  All calls share the one array: calls that overlap on the GPU
- * (other streams, other host threads) race on it, so serialise them.
- * Blocks until the stream has finished; returns BSS_ERR_NOT_SPD on a failed
- * pivot. */
+ * is launched, as are N >= 2^40 and k > INT32_MAX.  The first call on a
+ * device looks up the array's device address with that device current and
+ * keeps it for the life of the process; make that first call before any
+ * stream capture, and do not call this entry point on a device after
+ * cudaDeviceReset (the kept address belonged to the reset context).  All
+ * calls share the one array: calls that overlap on the GPU (other streams,
+ * other host threads) race on it, so serialise them.  Blocks until the
+ * stream has finished; returns BSS_ERR_NOT_SPD on a failed pivot and
+ * BSS_ERR_TIMEOUT when a bounded tensor-core wait of the wide FP32 path
+ * (64 < n <= 128) expired (the result is then void). */
 #define BSS_NOALLOC_SCRATCH_BYTES (8u << 20)
 int bss_factor_solve_noalloc(int64_t N, int64_t n, int64_t k, int32_t dtype, void *A, void *B, void *d,
                              void *stream);
@@ -424,6 +432,13 @@ int bss_diag_residual(int64_t N, int64_t n, int64_t k, int32_t method, const dou
  * most `polls` (1 .. 2^18) polls.  *timed_out = 1 when the wait gave up (as
  * it must), *cycles = the SM clock cycles it took.  Synchronises. */
 int bss_diag_wait_timeout(int64_t polls, int64_t *timed_out, int64_t *cycles);
+
+/* Diagnostic (no counterpart in the reference): the FMA-pipe peak of the
+ * current GPU in TFLOP/s for BSS_F32 or BSS_F64 (one FMA = 2 flops), measured
+ * by a kernel of independent FMA chains on every SM (best of three timed
+ * launches, CUDA events).  The benchmark's roofline fractions use it as the
+ * compute peak of the FP32 and FP64 paths.  Synchronises the device. */
+int bss_diag_fma_peak(int32_t dtype, double *tflops);
 
 /* Number of CUDA kernels this library has launched in this process, over
  * all handles (no counterpart in the reference; benchmarks report it). */

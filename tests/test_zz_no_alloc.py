@@ -56,6 +56,65 @@ def test_noalloc_matches_handle_path_twice(T):
         assert O.rel_error(x, O.cpu_solve(A, B, d)) <= TOL[T]
 
 
+def _noalloc(L, _lib, N, n, k, T, A, B, d, torch):
+    """one call of the no-allocation entry point on fresh caller-owned
+    buffers; B may be None (N = 1) and is then passed as NULL"""
+    dt = torch.float64 if T == "f64" else torch.float32
+    code = _lib.BSS_F64 if T == "f64" else _lib.BSS_F32
+    Ad, dd = _colmajor(A, dt, torch), _colmajor(d, dt, torch)
+    Bd = _colmajor(B, dt, torch) if B is not None else None
+    torch.cuda.synchronize()
+    rc = L.bss_factor_solve_noalloc(N, n, k, code, ctypes.c_void_p(Ad.data_ptr()),
+                                    ctypes.c_void_p(Bd.data_ptr() if Bd is not None else None),
+                                    ctypes.c_void_p(dd.data_ptr()),
+                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(rc)
+    return np.swapaxes(dd.double().cpu().numpy(), 1, 2)
+
+
+# paths of the entry point that differ from the two cases above: the wide
+# tile-streamed kernels (n > 64; FP32 n <= 128 on the tensor cores), a single
+# sequential level (N <= 8), N = 1 with no B buffer, and more right-hand
+# sides than one solve pass takes (several column chunks)
+@pytest.mark.parametrize("T", ["f64", "f32"])
+@pytest.mark.parametrize("seed,N,n,k", [(4, 20, 96, 2), (5, 5, 32, 1), (6, 1, 16, 3), (7, 60, 16, 40)],
+                         ids=["wide_n96", "seq_N5", "single_N1", "chunks_k40"])
+def test_noalloc_other_paths_twice(T, seed, N, n, k):
+    import torch
+    import blockstructuredsolvers_gb300 as bss
+    from blockstructuredsolvers_gb300 import _lib
+    L = _lib.load()
+    dt = torch.float64 if T == "f64" else torch.float32
+    rng = np.random.default_rng(seed)
+    A, B, d = O.gen_shifted_family(rng, N, n, k, diag_shift=2.0 * n, b_scale=0.5)
+    data = bss.initialize_batched(N, n, dt, k=k)
+    upload(data, A, B, d)
+    bss.factorize_(data)
+    bss.solve_(data)
+    bss.synchronize(data)
+    x_ref = download_x(data, N)
+    x_cpu = O.cpu_solve(A, B, d)
+    for call in range(2):  # the second call runs on the array the first one left behind
+        x = _noalloc(L, _lib, N, n, k, T, A, B if N > 1 else None, d, torch)
+        assert O.rel_error(x, x_ref) <= TOL[T], (call, O.rel_error(x, x_ref))
+        assert O.rel_error(x, x_cpu) <= TOL[T]
+
+
+def test_noalloc_rejects_out_of_range_sizes():
+    """sizes that would not survive the narrowing to the kernels' int
+    arguments are rejected before anything runs"""
+    import torch
+    from blockstructuredsolvers_gb300 import _lib
+    L = _lib.load()
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    buf = torch.zeros(16, dtype=torch.float64, device="cuda")
+    p = ctypes.c_void_p(buf.data_ptr())
+    assert L.bss_factor_solve_noalloc(4, (1 << 32) + 16, 1, _lib.BSS_F64, p, p, p, s) != _lib.BSS_OK
+    assert L.bss_factor_solve_noalloc(4, 16, (1 << 31) + 1, _lib.BSS_F64, p, p, p, s) == _lib.BSS_ERR_ARG
+    assert L.bss_factor_solve_noalloc(1 << 41, 16, 1, _lib.BSS_F64, p, p, p, s) == _lib.BSS_ERR_ARG
+    assert torch.count_nonzero(buf).item() == 0
+
+
 def test_noalloc_rejects_oversize_and_reports_not_spd():
     import torch
     from blockstructuredsolvers_gb300 import _lib
