@@ -13,6 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libbss_gb300.so")
 
 BSS_OK = 0
+BSS_FACTOR_FMA_CHAIN = 1
 BSS_ERR_ARG = 1
 BSS_ERR_OOM = 2
 BSS_ERR_CUDA = 3
@@ -44,7 +45,7 @@ EXPORTS = (
     "bss_autotune", "bss_autotune_lookup", "bss_autotune_clear", "bss_autotune_save", "bss_autotune_load",
     "bss_cpu_create", "bss_cpu_destroy", "bss_cpu_get_tensors", "bss_cpu_factorize", "bss_cpu_solve",
     "bss_cpu_failed_block", "bss_tc_selftest", "bss_diag_wide_occupancy", "bss_diag_residual",
-    "bss_diag_wait_timeout", "bss_diag_fma_peak",
+    "bss_diag_wait_timeout", "bss_diag_fma_peak", "bss_diag_set_factor_variant", "bss_diag_get_factor_variant",
     "bss_refalgo_create", "bss_refalgo_destroy", "bss_refalgo_get_tensors", "bss_refalgo_get_dims",
     "bss_refalgo_factorize", "bss_refalgo_solve",
     "bss_csr_nnz", "bss_csr_assemble", "bss_spchol_create", "bss_spchol_destroy", "bss_spchol_get_tensors",
@@ -115,6 +116,7 @@ class TuneEntry(ctypes.Structure):
         ("chain_blocks", ctypes.c_int32),
         ("single_ms", ctypes.c_double),
         ("batch_ms", ctypes.c_double),
+        ("factor_variant", ctypes.c_int32),
     ]
 
 
@@ -219,6 +221,9 @@ def load(path: str | None = None):
     L.bss_diag_residual.argtypes = [i64, i64, i64, i32, vp, vp, vp, vp, vp, vp]
     L.bss_diag_wait_timeout.argtypes = [i64, ctypes.POINTER(i64), ctypes.POINTER(i64)]
     L.bss_diag_fma_peak.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
+    L.bss_diag_set_factor_variant.argtypes = [i32]
+    L.bss_diag_get_factor_variant.argtypes = []
+    L.bss_diag_get_factor_variant.restype = i32
     L.bss_refalgo_create.argtypes = [i64, i64, i64, i32, vp, ctypes.POINTER(vp)]
     L.bss_refalgo_destroy.argtypes = [vp]
     L.bss_refalgo_get_tensors.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]

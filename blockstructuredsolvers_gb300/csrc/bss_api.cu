@@ -174,11 +174,11 @@ struct ArenaPlan {
     }
 };
 
-int chain_ctas_per_sm(int tin, int t, int n)
+int chain_ctas_per_sm(int tin, int t, int n, int variant)
 {
-    if (tin == F64 && t == F32) return chain_factor_ctas_per_sm<double, float>(n);
-    if (t == F32) return chain_factor_ctas_per_sm<float, float>(n);
-    return chain_factor_ctas_per_sm<double, double>(n);
+    if (tin == F64 && t == F32) return chain_factor_ctas_per_sm<double, float>(n, variant);
+    if (t == F32) return chain_factor_ctas_per_sm<float, float>(n, variant);
+    return chain_factor_ctas_per_sm<double, double>(n, variant);
 }
 
 }  // namespace
@@ -190,6 +190,11 @@ int bss::plan_handle(bss_handle *h)
     const int D = h->dtype;
     std::vector<long long> Ns, Qs;
     long long coarsest = h->N;
+    {
+        // kernel variant: the autotuner's choice for (n, dtype, precision), else the default
+        bss_tune_entry tv{};
+        h->variant = tuned_plan((int)n, D, h->opt.precision, &tv) ? tv.factor_variant : default_factor_variant();
+    }
     if (!h->seq_api) {
         if (h->opt.plan == BSS_PLAN_REFERENCE) {
             std::vector<long long> Nl, ml, Pl;
@@ -206,7 +211,7 @@ int bss::plan_handle(bss_handle *h)
             const int tin0 = D;
             bss_tune_entry te{};
             const bool tuned = tuned_plan((int)n, D, h->opt.precision, &te);
-            const long long wave = (long long)sms * chain_ctas_per_sm(tin0, t0, (int)n);
+            const long long wave = (long long)sms * chain_ctas_per_sm(tin0, t0, (int)n, h->variant);
             long long target = h->opt.target_partitions > 0
                                    ? h->opt.target_partitions
                                    : (tuned ? std::max(1LL, wave * te.wave_mult_x4 / 4) : wave);
@@ -497,6 +502,7 @@ ChainFactorArgs<Tin, T> bss::make_factor_args(bss_handle *h, int l)
     a.seq = L.seq ? 1 : 0;
     a.level = l;
     a.st = h->st;
+    a.variant = h->variant;
     return a;
 }
 template ChainFactorArgs<double, double> bss::make_factor_args<double, double>(bss_handle *, int);

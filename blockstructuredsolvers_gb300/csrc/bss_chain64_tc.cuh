@@ -1,0 +1,418 @@
+// Chain factor kernel for 64-wide blocks (n in 33..64) with FP32 factors on
+// the 5th-generation tensor cores: one CTA walks one partition's chain like
+// chain_factor_body (same recursion, same outputs V_i, W_i, Y_i and
+// S_LL / S_RR / S_LR), with every product of a chain step on tcgen05.mma and
+// the block loads on the bulk-copy (TMA) engine.
+//
+// Products (K = 64, 3xTF32: x = hi + lo, C = Xh Yh + Xh Yl + Xl Yh in the FP32
+// TMEM accumulator, relative error ~2^-21 like FP32 FMA products).  Each is one
+// M = 128, N = 64 MMA sequence whose A operand stacks two 64-row operands:
+//   P1 = [W_{i-1} | Y_{i-1}]^T W_{i-1}   rows 0-63:   W^T W       -> Ahat_i = A_i - W^T W
+//                                          rows 64-127: Y^T W       -> Z_i = -(Y^T W)^T
+//   P3 = [W_{i-1} | Y_{i-1}]^T Y_{i-1}   rows 64-127: Y^T Y, accumulated in TMEM
+//                                          over the chain (S_LL); rows 0-63 unused
+//   P2 = [Z_i | B_i]^T V_i                rows 0-63:   Z^T V = Y_i^T
+//                                          rows 64-127: B^T V = W_i^T
+// and at the chain end P1 on [W_last | Y_last] gives S_RR = W^T W and
+// S_LR = Y^T W.  Reference: the potrf/trsm/gemm sequence of
+// cholesky_factorize_batched! and the Schur products of
+// compute_schur_complement! (src/backbone_cuda.jl:70-101, 143-157).
+//
+// Shared memory (100.7 KB: two CTAs per SM):
+//   R   64 KB  the stacked A operand, canonical no-swizzle K-major layout with
+//              the hi and lo parts interleaved per 8-row group: element
+//              (row, k) of part h at (row/8)*4096 + h*2048 + (k/4)*128 +
+//              (row%8)*16 + (k%4)*4 (leading byte offset 128, stride byte
+//              offset 4096), so rows 64-127 (hi and lo) are the contiguous
+//              upper 32 KB, where B_i lands raw from HBM before conversion
+//   VR  34 KB  the Cholesky tiles sS, sV (padded column-major, as
+//              chol_inv_blocked wants them); after the Cholesky the V operand
+//              (same canonical layout, 32 KB); between steps the raw A_{i+1}
+// TMEM: 128 columns: 0-63 the P1/P2 accumulator, 64-127 S_LL.
+//
+// Block loads: A_{i+1} (into VR, issued once P2 of step i has read V) and
+// B_i (into R's upper half, issued once P1 of step i has read R) are single
+// cp.async.bulk copies completing on mbarriers; both blocks are prefetched
+// into L2 (cp.async.bulk.prefetch.L2) a whole step ahead.  B_i's copy
+// overlaps the Cholesky.  Blocks whose byte size is not a multiple of 16
+// (odd n) are read with plain loads instead.
+//
+// Every mbarrier wait is bounded (TC_WAIT_LIMIT polls); an expired wait sets
+// an abort flag, the CTA stops its chain, waits (bounded) for its copies and
+// MMAs still in flight, frees its TMEM and records the timeout in the status.
+#pragma once
+
+namespace bss {
+
+constexpr int C64_R_BYTES = 65536;
+constexpr int C64_VR_BYTES = 2 * Geo<float, 64>::SLOT * 4;  // sS + sV = 34816
+constexpr int C64_THREADS = 256;
+
+constexpr size_t chain64_tc_smem() { return (size_t)C64_R_BYTES + C64_VR_BYTES + 256 + 64; }
+
+__device__ __forceinline__ uint32_t c64_off(int row, int k, int part)
+{
+    return (uint32_t)((row >> 3) * 4096 + part * 2048 + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4);
+}
+
+__device__ __forceinline__ uint64_t c64_desc(uint32_t saddr)
+{
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)(128u >> 4) << 16;   // leading byte offset: next core matrix along K
+    d |= (uint64_t)(4096u >> 4) << 32;  // stride byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;             // descriptor version of the sm_100 family
+    return d;
+}
+
+// kind::tf32, D = F32, A = B = TF32, both K-major, M = 128, N = 64
+__host__ __device__ constexpr uint32_t c64_idesc()
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+// TMEM cols at tm (+)= Aop(128 rows at shared address a) x Bop(64 rows at b)^T
+// over K = 64 in 3xTF32; issued by one thread
+__device__ __forceinline__ void c64_mma(uint32_t tm, uint32_t a, uint32_t b, bool accumulate)
+{
+    constexpr uint32_t id = c64_idesc();
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+        const uint32_t o = (uint32_t)kk * 256u;  // K = 8: two core matrices along K
+        const uint64_t ah = c64_desc(a + o), al = c64_desc(a + 2048u + o);
+        const uint64_t bh = c64_desc(b + o), bl = c64_desc(b + 2048u + o);
+        tc_mma(tm, ah, bh, id, (accumulate || kk) ? 1u : 0u);
+        tc_mma(tm, ah, bl, id, 1u);
+        tc_mma(tm, al, bh, id, 1u);
+    }
+}
+
+// four consecutive K values (k4 .. k4+3) of one operand row, split hi / lo
+__device__ __forceinline__ void c64_put4(unsigned char *base, int row, int k4, float a, float b, float c, float d)
+{
+    const uint32_t h0 = to_tf32(a), h1 = to_tf32(b), h2 = to_tf32(c), h3 = to_tf32(d);
+    const uint32_t l0 = to_tf32(a - __uint_as_float(h0)), l1 = to_tf32(b - __uint_as_float(h1));
+    const uint32_t l2 = to_tf32(c - __uint_as_float(h2)), l3 = to_tf32(d - __uint_as_float(h3));
+    *reinterpret_cast<uint4 *>(base + c64_off(row, k4, 0)) = make_uint4(h0, h1, h2, h3);
+    *reinterpret_cast<uint4 *>(base + c64_off(row, k4, 1)) = make_uint4(l0, l1, l2, l3);
+}
+
+// 32 consecutive accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void c64_ld32(uint32_t addr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+          "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+          "=r"(r[30]), "=r"(r[31])
+        : "r"(addr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+// one bulk copy global -> shared (16-byte aligned, size a multiple of 16),
+// completing `bytes` of transaction count on the mbarrier
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
+// an outstanding mbarrier phase: wait for it (bounded); on expiry set the
+// abort flag and leave the phase outstanding (drained before exit)
+struct C64Bar {
+    uint32_t addr;
+    uint32_t phase;
+    bool pending;
+};
+
+__device__ __forceinline__ void c64_wait(C64Bar &b, int *abort)
+{
+    if (!b.pending) return;
+    if (mbar_wait(b.addr, b.phase)) {
+        b.phase ^= 1u;
+        b.pending = false;
+    } else {
+        *abort = 1;
+    }
+}
+
+template <class Tin>
+__global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorArgs<Tin, float> g)
+{
+    constexpr int LD = Geo<float, 64>::LD;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned char *R = smem_raw;
+    unsigned char *VR = smem_raw + C64_R_BYTES;
+    float *sS = reinterpret_cast<float *>(VR);
+    float *sV = sS + Geo<float, 64>::SLOT;
+    float *dinv = reinterpret_cast<float *>(VR + C64_VR_BYTES);
+    unsigned char *tail = VR + C64_VR_BYTES + 256;
+    int *sflag = reinterpret_cast<int *>(tail);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(tail + 4);
+    int *abort = reinterpret_cast<int *>(tail + 8);
+    uint64_t *mbars = reinterpret_cast<uint64_t *>(tail + 16);  // MMA, A copy, B copy
+    const Tin *rawA = reinterpret_cast<const Tin *>(VR);
+    const Tin *rawB = reinterpret_cast<const Tin *>(R + 32768);
+
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int L = 32 * (w & 3) + lane;  // this thread's TMEM lane (accumulator row)
+    const int c0 = 32 * (w >> 2);       // its first accumulator column
+    const uint32_t lane_base = (uint32_t)(32 * (w & 3)) << 16;
+    const int n = g.n;
+    const long long nn = (long long)n * n;
+    const long long p = blockIdx.x;
+    const long long sL = (p * (g.N - 1)) / g.Q;
+    const long long sR = ((p + 1) * (g.N - 1)) / g.Q;
+    const long long first = sL + 1, last = sR - 1;
+    const uint32_t blk_bytes = (uint32_t)(nn * (long long)sizeof(Tin));
+    const bool bulk = (blk_bytes % 16u) == 0 && ((uintptr_t)g.A_in % 16u) == 0 && ((uintptr_t)g.B_in % 16u) == 0;
+
+    if (w == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"(128u)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int q = 0; q < 3; ++q)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbars[q])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *abort = 0;
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tm = *tslot;
+    const uint32_t sRa = smem_u32(R), sVa = smem_u32(VR);
+    C64Bar bM{smem_u32(&mbars[0]), 0u, false}, bA{smem_u32(&mbars[1]), 0u, false}, bB{smem_u32(&mbars[2]), 0u, false};
+
+    if (first <= last && bulk) {
+        if (tid == 0) {
+            mbar_expect_tx(bA.addr, blk_bytes);
+            bulk_g2s(sVa, g.A_in + first * nn, blk_bytes, bA.addr);
+            bulk_prefetch_l2(g.B_in + first * nn, blk_bytes);
+        }
+        bA.pending = true;
+    }
+    bool sll_started = false;
+    for (long long i = first; i <= last; ++i) {
+        const long long t = i - first;
+        // ---- P1 and P3 on [W_{i-1} | Y_{i-1}] (written and fenced by the previous step)
+        if (t > 0) {
+            if (tid == 0) {
+                tc_fence_after();
+                c64_mma(tm, sRa, sRa, false);
+                c64_mma(tm + 64u, sRa, sRa + 32768u, sll_started);
+                tc_commit(bM.addr);
+            }
+            bM.pending = true;
+            sll_started = true;
+        }
+        if (tid == 32 && bulk && i < last) {  // the next step's blocks into L2
+            bulk_prefetch_l2(g.A_in + (i + 1) * nn, blk_bytes);
+            bulk_prefetch_l2(g.B_in + (i + 1) * nn, blk_bytes);
+        }
+        c64_wait(bM, abort);
+        // R has been read: B_i raw into its upper half (it lands during the Cholesky)
+        if (bulk) {
+            if (tid == 0) {
+                fence_async_smem();
+                mbar_expect_tx(bB.addr, blk_bytes);
+                bulk_g2s(sRa + 32768u, g.B_in + i * nn, blk_bytes, bB.addr);
+            }
+            bB.pending = true;
+        }
+        c64_wait(bA, abort);
+        tc_fence_after();
+        // ---- Ahat_i (rows L < 64) and Z_i (rows L >= 64) from the P1 accumulator
+        float dv[32];
+        if (t > 0) {
+            c64_ld32(tm + lane_base + (uint32_t)c0, dv);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 32; ++q) dv[q] = 0.f;
+        }
+        if (L < 64) {  // dv <- Ahat row L (identity outside n x n)
+            const Tin *Ag = g.A_in + i * nn;
+#pragma unroll
+            for (int q = 0; q < 32; ++q) {
+                const int c = c0 + q;
+                dv[q] = (L < n && c < n) ? (float)(bulk ? rawA[L + c * n] : Ag[L + (long long)c * n]) - dv[q]
+                                         : (L == c ? 1.f : 0.f);
+            }
+        }
+        __syncthreads();  // every read of the raw A_i is done before sS (same bytes) is written
+        if (L < 64) {
+#pragma unroll
+            for (int q = 0; q < 32; ++q) sS[L + (c0 + q) * LD] = dv[q];
+        } else if (t > 0) {
+            const int cz = L - 64;  // column cz of Z = row cz of the P2 operand
+#pragma unroll
+            for (int q = 0; q < 32; q += 4) {
+                float z[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) z[u] = (cz < n && c0 + q + u < n) ? -dv[q + u] : 0.f;
+                c64_put4(R, cz, c0 + q, z[0], z[1], z[2], z[3]);
+            }
+        }
+        if (t == 0) {
+            // Z_first = B_sL^T: row r of the operand (column r of Z) is row r of B_sL
+            const int row = tid >> 2, k0 = (tid & 3) * 16;
+            const Tin *Bs = g.B_in + sL * nn;
+#pragma unroll
+            for (int q = 0; q < 16; q += 4) {
+                float z[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int k = k0 + q + u;
+                    z[u] = (row < n && k < n) ? (float)Bs[row + (long long)k * n] : 0.f;
+                }
+                c64_put4(R, row, k0 + q, z[0], z[1], z[2], z[3]);
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        if (*abort) break;
+        // ---- U^T U = Ahat, V = U^-1 (CUDA cores; ends with a CTA barrier)
+        const int bad = chol_inv_blocked<float, 64, C64_THREADS>(sS, sV, dinv, sflag, tid);
+        if (bad && tid == 0) record_bad_pivot(g.st, g.level, i);
+        // ---- V_i to HBM, and the V_i and B_i operands
+        c64_wait(bB, abort);
+        {
+            const int j = tid >> 2, k0 = (tid & 3) * 16;
+            float vv[16], bv[16];
+            const Tin *Bg = g.B_in + i * nn;
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int k = k0 + q;
+                vv[q] = ((k >> 4) > (j >> 4)) ? 0.f : sV[k + j * LD];  // V's lower tiles are zero
+                bv[q] = (j < n && k < n) ? (float)(bulk ? rawB[k + j * n] : Bg[k + (long long)j * n]) : 0.f;
+            }
+            float *Vg = g.A_f + i * nn;
+            if (n == 64) {
+#pragma unroll
+                for (int q = 0; q < 16; q += 4)
+                    *reinterpret_cast<float4 *>(Vg + j * 64 + k0 + q) = make_float4(vv[q], vv[q + 1], vv[q + 2], vv[q + 3]);
+            } else if (j < n) {
+#pragma unroll
+                for (int q = 0; q < 16; ++q)
+                    if (k0 + q < n) Vg[(long long)j * n + k0 + q] = vv[q];
+            }
+            __syncthreads();  // sV and the raw B_i are read: their bytes become operands
+#pragma unroll
+            for (int q = 0; q < 16; q += 4) {
+                c64_put4(VR, j, k0 + q, vv[q], vv[q + 1], vv[q + 2], vv[q + 3]);
+                c64_put4(R, 64 + j, k0 + q, bv[q], bv[q + 1], bv[q + 2], bv[q + 3]);
+            }
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (*abort) break;
+        // ---- P2 = [Z_i | B_i]^T V_i
+        if (tid == 0) {
+            tc_fence_after();
+            c64_mma(tm, sRa, sVa, false);
+            tc_commit(bM.addr);
+        }
+        bM.pending = true;
+        c64_wait(bM, abort);
+        tc_fence_after();
+        if (bulk && i < last) {  // V has been read: the next A block into VR
+            if (tid == 0) {
+                fence_async_smem();
+                mbar_expect_tx(bA.addr, blk_bytes);
+                bulk_g2s(sVa, g.A_in + (i + 1) * nn, blk_bytes, bA.addr);
+            }
+            bA.pending = true;
+        }
+        // ---- Y_i (rows L < 64) and W_i (rows L >= 64): to HBM and into R as [W_i | Y_i]
+        c64_ld32(tm + lane_base + (uint32_t)c0, dv);
+        {
+            const bool isY = L < 64;
+            const int col = isY ? L : L - 64;
+            float *dst = (isY ? g.Y : g.B_f) + i * nn;
+            if (n == 64) {
+#pragma unroll
+                for (int q = 0; q < 32; q += 4)
+                    *reinterpret_cast<float4 *>(dst + col * 64 + c0 + q) = make_float4(dv[q], dv[q + 1], dv[q + 2], dv[q + 3]);
+            } else if (col < n) {
+#pragma unroll
+                for (int q = 0; q < 32; ++q)
+                    if (c0 + q < n) dst[(long long)col * n + c0 + q] = dv[q];
+            }
+            const int row = isY ? 64 + col : col;
+#pragma unroll
+            for (int q = 0; q < 32; q += 4) c64_put4(R, row, c0 + q, dv[q], dv[q + 1], dv[q + 2], dv[q + 3]);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (*abort) break;
+    }
+
+    // ---- chain end: S_RR = W^T W, S_LR = Y^T W (P1) and the last S_LL term (P3)
+    if (!*abort && first <= last) {
+        if (tid == 0) {
+            tc_fence_after();
+            c64_mma(tm, sRa, sRa, false);
+            c64_mma(tm + 64u, sRa, sRa + 32768u, sll_started);
+            tc_commit(bM.addr);
+        }
+        bM.pending = true;
+        c64_wait(bM, abort);
+        tc_fence_after();
+        float dv[32];
+        float *Cp = g.C + p * 3 * nn;
+        c64_ld32(tm + lane_base + (uint32_t)c0, dv);
+        {
+            const int r = L < 64 ? L : L - 64;
+            float *dst = Cp + (L < 64 ? nn : 2 * nn);  // S_RR rows, S_LR rows
+            if (r < n) {
+#pragma unroll
+                for (int q = 0; q < 32; ++q)
+                    if (c0 + q < n) dst[r + (long long)(c0 + q) * n] = dv[q];
+            }
+        }
+        c64_ld32(tm + lane_base + 64u + (uint32_t)c0, dv);
+        if (L >= 64 && L - 64 < n) {
+            const int r = L - 64;
+#pragma unroll
+            for (int q = 0; q < 32; ++q)
+                if (c0 + q < n) Cp[r + (long long)(c0 + q) * n] = dv[q];
+        }
+    }
+    __syncthreads();
+    if (*abort) {
+        // a wait gave up: wait (bounded) for this CTA's copies and MMAs still
+        // in flight before its shared memory and TMEM are released
+        if (bM.pending) mbar_wait(bM.addr, bM.phase);
+        if (bA.pending) mbar_wait(bA.addr, bA.phase);
+        if (bB.pending) mbar_wait(bB.addr, bB.phase);
+        if (tid == 0 && g.st) atomicExch(&g.st->tc_timeout, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (w == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(128u) : "memory");
+    }
+}
+
+}  // namespace bss

@@ -249,3 +249,13 @@ extern "C" int bss_diag_fma_peak(int32_t dtype, double *tflops)
     if (dtype == BSS_F32) return fma_peak<float>(tflops);
     return fail(BSS_ERR_ARG, "bss_diag_fma_peak: dtype must be BSS_F32 or BSS_F64");
 }
+
+extern "C" int bss_diag_set_factor_variant(int32_t variant)
+{
+    if (variant < 0 || variant > FACTOR_FMA_CHAIN)
+        return fail(BSS_ERR_ARG, "bss_diag_set_factor_variant: 0 or BSS_FACTOR_FMA_CHAIN");
+    set_default_factor_variant(variant);
+    return BSS_OK;
+}
+
+extern "C" int32_t bss_diag_get_factor_variant(void) { return default_factor_variant(); }

@@ -66,6 +66,7 @@ struct bss_handle {
     bool factored = false;
     bool need_anorm = false;  // the next residual also computes ||T||_inf
     int kc_max = 1;
+    int variant = 0;  // FACTOR_* kernel variant bits of this handle's factorization
     bss_info info{};
     int sticky = BSS_OK;
     // CUDA graphs: the first call of each kind runs eagerly on `stream`; later

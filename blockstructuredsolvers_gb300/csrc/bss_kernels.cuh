@@ -561,6 +561,13 @@ struct ChainFactorArgs {
     int seq;          // 1: one chain over all blocks, no separators
     int level;
     DevStatus *st;
+    int variant;      // FACTOR_* bits: which kernel factors the chain
+};
+
+// kernel variants of a factorization (bits of ChainFactorArgs::variant),
+// chosen per handle (the defaults, or the autotuner's choice per (n, dtype))
+enum {
+    FACTOR_FMA_CHAIN = 1,  // 33 <= n <= 64, FP32 factors: CUDA-core chain kernel instead of the tensor-core one
 };
 
 template <class T, int NB>
@@ -2674,3 +2681,5 @@ __global__ void init_identity_kernel(T *A, long long first_blk, long long last_b
 }
 
 }  // namespace bss
+
+#include "bss_chain64_tc.cuh"

@@ -21,7 +21,12 @@ int tile_for(int n);  // NB in {16, 32, 64}, WIDE_CLASS, or 0 if unsupported
 template <class Tin, class T>
 cudaError_t launch_chain_factor(const ChainFactorArgs<Tin, T> &a, cudaStream_t s);
 template <class Tin, class T>
-int chain_factor_ctas_per_sm(int n);
+int chain_factor_ctas_per_sm(int n, int variant);
+
+// FACTOR_* variant bits that handles take when the autotuner has no entry
+// for their (n, dtype, precision); process-wide
+int default_factor_variant();
+void set_default_factor_variant(int v);
 
 template <class Tsrc, class T, class Tdst>
 cudaError_t launch_assemble_schur(const Tsrc *A_src, const T *C, Tdst *A_next, Tdst *B_next, long long N,

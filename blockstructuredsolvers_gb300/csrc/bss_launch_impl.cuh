@@ -13,9 +13,27 @@ inline int grid_for(long long work, int threads, int cap = 152 * 16)
     return (int)g;
 }
 
+// partitioned levels of 64-wide blocks with FP32 factors: the tensor-core
+// chain kernel (bss_chain64_tc.cuh), unless the CUDA-core variant is chosen
+template <class Tin>
+static cudaError_t chain64_tc(const ChainFactorArgs<Tin, float> &a, cudaStream_t s)
+{
+    const size_t smem = chain64_tc_smem();
+    auto kern = chain64_tc_kernel<Tin>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    kern<<<(unsigned)a.Q, C64_THREADS, smem, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
 template <class Tin, class T, int NB>
 static cudaError_t chain_factor_nb(const ChainFactorArgs<Tin, T> &a, cudaStream_t s)
 {
+    if constexpr (std::is_same<T, float>::value && NB == 64) {
+        if (!a.seq && !(a.variant & FACTOR_FMA_CHAIN)) return chain64_tc<Tin>(a, s);
+    }
     const size_t smem = chain_factor_smem<T, NB>();
     auto kern = chain_factor_kernel<Tin, T, NB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -62,8 +80,18 @@ cudaError_t launch_chain_factor(const ChainFactorArgs<Tin, T> &a, cudaStream_t s
 }
 
 template <class Tin, class T, int NB>
-static int ctas_nb()
+static int ctas_nb(int variant)
 {
+    if constexpr (std::is_same<T, float>::value && NB == 64) {
+        if (!(variant & FACTOR_FMA_CHAIN)) {
+            const size_t smem = chain64_tc_smem();
+            auto kern = chain64_tc_kernel<Tin>;
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+                return 1;
+            cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+            return ctas_per_sm(kern, C64_THREADS, smem);
+        }
+    }
     const size_t smem = chain_factor_smem<T, NB>();
     auto kern = chain_factor_kernel<Tin, T, NB>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
@@ -84,12 +112,12 @@ static int wide_ctas_tc()
 }
 
 template <class Tin, class T>
-int chain_factor_ctas_per_sm(int n)
+int chain_factor_ctas_per_sm(int n, int variant)
 {
     switch (tile_for(n)) {
-    case 16: return ctas_nb<Tin, T, 16>();
-    case 32: return ctas_nb<Tin, T, 32>();
-    case 64: return ctas_nb<Tin, T, 64>();
+    case 16: return ctas_nb<Tin, T, 16>(variant);
+    case 32: return ctas_nb<Tin, T, 32>(variant);
+    case 64: return ctas_nb<Tin, T, 64>(variant);
     case WIDE_CLASS:
         if constexpr (std::is_same<T, float>::value) {
             if (wide_uses_tc<T>(n)) return wide_ctas_tc<Tin, T, true>();

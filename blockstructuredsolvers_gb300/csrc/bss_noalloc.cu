@@ -162,6 +162,7 @@ int run(long long N, int n, int k, T *A, T *B, T *d, cudaStream_t s)
         a.seq = lv[l].seq ? 1 : 0;
         a.level = l;
         a.st = st;
+        a.variant = default_factor_variant();
         NA_CHECK((launch_chain_factor<T, T>(a, s)));
         if (!lv[l].seq)
             NA_CHECK((launch_assemble_schur<T, T, T>((const T *)lv[l].A, (const T *)lv[l].C, (T *)lv[l + 1].A,

@@ -1,9 +1,11 @@
-// Autotuner of the recursion plan per (n, dtype, precision).  The kernels'
-// tile shapes and CTA sizes are fixed per block-size class (Tile<16/32/64>,
-// the wide path); what changes the run time for a given n is the plan: how
-// many partitions the finest level gets (in units of one wave of resident
-// chain CTAs), where the halving levels stop (the sequential cutoff), and,
-// for many-system batches, the chain length per partition.  The tuner times
+// Autotuner of the chain kernel and the recursion plan per (n, dtype,
+// precision).  Kernel: for FP32 factors of 33..64-wide blocks, the
+// tensor-core chain kernel (one 128-row tcgen05 tile, bulk-copied block
+// tiles, 100 KB of shared memory per CTA) or the CUDA-core one (4 x 4
+// register tiles over 256 threads, 105 KB).  Plan: how many partitions the
+// finest level gets (in units of one wave of resident CTAs of the chosen
+// kernel), where the halving levels stop (the sequential cutoff), and, for
+// many-system batches, the chain length per partition.  The tuner times
 // factorize+solve of a device-generated SPD system for each candidate with
 // CUDA events and keeps the fastest; results live in a process-wide table
 // (consulted by the planners whenever the caller leaves the corresponding
@@ -192,31 +194,51 @@ extern "C" int bss_autotune(int64_t n, int32_t dtype, int32_t precision, int64_t
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int t0 = precision == BSS_PRECISION_MIXED ? BSS_F32 : dtype;
-    int ctas = 1;
-    if (dtype == BSS_F64 && t0 == BSS_F32)
-        ctas = chain_factor_ctas_per_sm<double, float>((int)n);
-    else if (t0 == BSS_F32)
-        ctas = chain_factor_ctas_per_sm<float, float>((int)n);
-    else
-        ctas = chain_factor_ctas_per_sm<double, double>((int)n);
-    for (int m4 : mults4)
-        for (int c : cutoffs) {
-            bss_options o;
-            bss_default_options(&o);
-            o.precision = precision;
-            o.target_partitions = std::max(1, (sms * ctas * m4) / 4);
-            o.seq_cutoff = c;
-            double ms = 0.0;
-            const int rc = time_handle(N_probe, (int)n, dtype, o, 3, &ms);
-            if (rc) return rc;
-            if (ms < best_ms) {
-                best_ms = ms;
-                best.wave_mult_x4 = m4;
-                best.seq_cutoff = c;
+    // kernel variants worth timing: FP32 factors of 33..64-wide blocks have two chain kernels
+    std::vector<int> variants{0};
+    if (t0 == BSS_F32 && tile_for((int)n) == 64) variants = {0, FACTOR_FMA_CHAIN};
+    // candidates run with the process-wide default variant set to theirs and
+    // no table entry for this key (the default is restored afterwards)
+    const int saved_default = default_factor_variant();
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune.erase(std::make_tuple((int)n, (int)dtype, (int)precision));
+    }
+    int rc_all = BSS_OK;
+    for (int v : variants) {
+        set_default_factor_variant(v);
+        int ctas = 1;
+        if (dtype == BSS_F64 && t0 == BSS_F32)
+            ctas = chain_factor_ctas_per_sm<double, float>((int)n, v);
+        else if (t0 == BSS_F32)
+            ctas = chain_factor_ctas_per_sm<float, float>((int)n, v);
+        else
+            ctas = chain_factor_ctas_per_sm<double, double>((int)n, v);
+        for (int m4 : mults4)
+            for (int c : cutoffs) {
+                if (rc_all) break;
+                bss_options o;
+                bss_default_options(&o);
+                o.precision = precision;
+                o.target_partitions = std::max(1, (sms * ctas * m4) / 4);
+                o.seq_cutoff = c;
+                double ms = 0.0;
+                rc_all = time_handle(N_probe, (int)n, dtype, o, 3, &ms);
+                if (rc_all == BSS_OK && ms < best_ms) {
+                    best_ms = ms;
+                    best.wave_mult_x4 = m4;
+                    best.seq_cutoff = c;
+                    best.factor_variant = v;
+                }
             }
-        }
+    }
+    if (rc_all) {
+        set_default_factor_variant(saved_default);
+        return rc_all;
+    }
     best.single_ms = best_ms;
     // batch: chain length per partition (256 systems of 512 blocks)
+    set_default_factor_variant(best.factor_variant);  // the batch runs with the winner's kernel
     const int chains[] = {16, 32, 64, 128, 256};
     double best_b = 1e300;
     for (int ch : chains) {
@@ -226,12 +248,16 @@ extern "C" int bss_autotune(int64_t n, int32_t dtype, int32_t precision, int64_t
         o.chain_blocks = ch;
         double ms = 0.0;
         const int rc = time_batch(256, 512, (int)n, dtype, o, 2, &ms);
-        if (rc) return rc;
+        if (rc) {
+            set_default_factor_variant(saved_default);
+            return rc;
+        }
         if (ms < best_b) {
             best_b = ms;
             best.chain_blocks = ch;
         }
     }
+    set_default_factor_variant(saved_default);
     best.batch_ms = best_b;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -259,11 +285,11 @@ extern "C" int bss_autotune_save(const char *path)
     FILE *f = std::fopen(path, "w");
     if (!f) return fail(BSS_ERR_ARG, std::string("cannot write ") + path);
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    std::fprintf(f, "# n dtype precision wave_mult_x4 seq_cutoff chain_blocks single_ms batch_ms\n");
+    std::fprintf(f, "# n dtype precision wave_mult_x4 seq_cutoff chain_blocks single_ms batch_ms factor_variant\n");
     for (auto &kv : g_tune) {
         const bss_tune_entry &e = kv.second;
-        std::fprintf(f, "%d %d %d %d %d %d %.17g %.17g\n", e.n, e.dtype, e.precision, e.wave_mult_x4, e.seq_cutoff,
-                     e.chain_blocks, e.single_ms, e.batch_ms);
+        std::fprintf(f, "%d %d %d %d %d %d %.17g %.17g %d\n", e.n, e.dtype, e.precision, e.wave_mult_x4, e.seq_cutoff,
+                     e.chain_blocks, e.single_ms, e.batch_ms, e.factor_variant);
     }
     std::fclose(f);
     return BSS_OK;
@@ -280,9 +306,13 @@ extern "C" int bss_autotune_load(const char *path)
     while (std::fgets(line, sizeof line, f)) {
         if (line[0] == '#') continue;
         bss_tune_entry e{};
-        if (std::sscanf(line, "%d %d %d %d %d %d %lf %lf", &e.n, &e.dtype, &e.precision, &e.wave_mult_x4,
-                        &e.seq_cutoff, &e.chain_blocks, &e.single_ms, &e.batch_ms) == 8 &&
-            e.n > 0 && e.wave_mult_x4 > 0 && e.seq_cutoff > 0 && e.chain_blocks > 0) {
+        // 9 columns; files written before the variant column have 8 (variant 0)
+        const int got = std::sscanf(line, "%d %d %d %d %d %d %lf %lf %d", &e.n, &e.dtype, &e.precision,
+                                    &e.wave_mult_x4, &e.seq_cutoff, &e.chain_blocks, &e.single_ms, &e.batch_ms,
+                                    &e.factor_variant);
+        if (got == 8) e.factor_variant = 0;
+        if ((got == 8 || got == 9) && e.n > 0 && e.wave_mult_x4 > 0 && e.seq_cutoff > 0 && e.chain_blocks > 0 &&
+            e.factor_variant >= 0 && e.factor_variant <= FACTOR_FMA_CHAIN) {
             g_tune[std::make_tuple(e.n, e.dtype, e.precision)] = e;
             ++loaded;
         }

@@ -4,7 +4,7 @@
 
 namespace bss {
 template cudaError_t launch_chain_factor<float, float>(const ChainFactorArgs<float, float> &, cudaStream_t);
-template int chain_factor_ctas_per_sm<float, float>(int);
+template int chain_factor_ctas_per_sm<float, float>(int, int);
 template cudaError_t launch_assemble_schur<float, float, float>(const float *, const float *, float *, float *,
                                                                 long long, long long, int, cudaStream_t);
 template cudaError_t launch_assemble_schur<float, float, double>(const float *, const float *, double *, double *,

@@ -3,7 +3,7 @@
 
 namespace bss {
 template cudaError_t launch_chain_factor<double, double>(const ChainFactorArgs<double, double> &, cudaStream_t);
-template int chain_factor_ctas_per_sm<double, double>(int);
+template int chain_factor_ctas_per_sm<double, double>(int, int);
 template cudaError_t launch_assemble_schur<double, double, double>(const double *, const double *, double *,
                                                                    double *, long long, long long, int,
                                                                    cudaStream_t);

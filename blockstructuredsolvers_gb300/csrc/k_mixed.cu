@@ -6,7 +6,7 @@
 
 namespace bss {
 template cudaError_t launch_chain_factor<double, float>(const ChainFactorArgs<double, float> &, cudaStream_t);
-template int chain_factor_ctas_per_sm<double, float>(int);
+template int chain_factor_ctas_per_sm<double, float>(int, int);
 template cudaError_t launch_assemble_schur<double, float, float>(const double *, const float *, float *, float *,
                                                                  long long, long long, int, cudaStream_t);
 template cudaError_t launch_assemble_schur<double, float, double>(const double *, const float *, double *,
@@ -42,6 +42,10 @@ cudaError_t launch_relres_control(DevStatus *st, double tol, int max_refine, cud
     count_launch();
     return cudaGetLastError();
 }
+
+static std::atomic<int> g_factor_variant{0};
+int default_factor_variant() { return g_factor_variant.load(std::memory_order_relaxed); }
+void set_default_factor_variant(int v) { g_factor_variant.store(v & FACTOR_FMA_CHAIN); }
 
 int tile_for(int n)
 {

@@ -342,6 +342,7 @@ typedef struct {
     int32_t chain_blocks;
     double single_ms;       /* best factorize+solve time of the probe system */
     double batch_ms;        /* best factorize+solve time of the probe batch  */
+    int32_t factor_variant; /* BSS_FACTOR_* bits of the chain kernel          */
 } bss_tune_entry;
 
 int bss_autotune(int64_t n, int32_t dtype, int32_t precision, int64_t N_probe, bss_tune_entry *out);
@@ -439,6 +440,18 @@ int bss_diag_wait_timeout(int64_t polls, int64_t *timed_out, int64_t *cycles);
  * launches, CUDA events).  The benchmark's roofline fractions use it as the
  * compute peak of the FP32 and FP64 paths.  Synchronises the device. */
 int bss_diag_fma_peak(int32_t dtype, double *tflops);
+
+/* Kernel variants of the chain factorization (bits; no counterpart in the
+ * reference).  BSS_FACTOR_FMA_CHAIN: partitioned levels of 33 <= n <= 64
+ * blocks with FP32 factors (plain FP32, and every level of the mixed path)
+ * run on the CUDA-core chain kernel instead of the tensor-core one (tcgen05
+ * 3xTF32 products, bulk-copied block tiles).  A handle takes the autotuner's
+ * variant for its (n, dtype, precision) when there is one, else the
+ * process-wide default set here (0 at start).  Applies to handles and
+ * batches created after the call. */
+#define BSS_FACTOR_FMA_CHAIN 1
+int bss_diag_set_factor_variant(int32_t variant);
+int32_t bss_diag_get_factor_variant(void);
 
 /* Number of CUDA kernels this library has launched in this process, over
  * all handles (no counterpart in the reference; benchmarks report it). */

@@ -24,7 +24,7 @@ def lib():
 def _declared():
     src = open(os.path.join(ROOT, "include", "bss.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(bss_[a-z_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(bss_[a-z0-9_]+)\s*\(", src)))
 
 
 def test_header_declares_core_entry_points():
