@@ -18,16 +18,20 @@
 // cholesky_factorize_batched! and the Schur products of
 // compute_schur_complement! (src/backbone_cuda.jl:70-101, 143-157).
 //
-// Shared memory (100.7 KB: two CTAs per SM):
-//   R   64 KB  the stacked A operand, canonical no-swizzle K-major layout with
-//              the hi and lo parts interleaved per 8-row group: element
-//              (row, k) of part h at (row/8)*4096 + h*2048 + (k/4)*128 +
-//              (row%8)*16 + (k%4)*4 (leading byte offset 128, stride byte
-//              offset 4096), so rows 64-127 (hi and lo) are the contiguous
-//              upper 32 KB, where B_i lands raw from HBM before conversion
-//   VR  34 KB  the Cholesky tiles sS, sV (padded column-major, as
+// Shared memory (108.3 KB: two CTAs per SM):
+//   R   72 KB  the stacked A operand in the no-swizzle K-major layout of
+//              8-row x 16-byte core matrices, with the hi and lo parts
+//              interleaved per 8-row group: element (row, k) of part h at
+//              (row/8)*4608 + h*2304 + (k/4)*144 + (row%8)*16 + (k%4)*4
+//              (leading byte offset 144, stride byte offset 4608).  The core
+//              matrices of a row group sit 144 bytes apart instead of 128, so
+//              eight threads writing the same row at eight consecutive k
+//              groups hit eight different bank groups (with 128 they would
+//              all hit one).  Rows 64-127 (hi and lo) are the contiguous upper
+//              36 KB, where B_i lands raw from HBM before conversion
+//   VR  36 KB  the Cholesky tiles sS, sV (padded column-major, as
 //              chol_inv_blocked wants them); after the Cholesky the V operand
-//              (same canonical layout, 32 KB); between steps the raw A_{i+1}
+//              (same layout); between steps the raw A_{i+1}
 // TMEM: 128 columns: 0-63 the P1/P2 accumulator, 64-127 S_LL.
 //
 // Block loads: A_{i+1} (into VR, issued once P2 of step i has read V) and
@@ -37,30 +41,38 @@
 // overlaps the Cholesky.  Blocks whose byte size is not a multiple of 16
 // (odd n) are read with plain loads instead.
 //
-// Every mbarrier wait is bounded (TC_WAIT_LIMIT polls); an expired wait sets
-// an abort flag, the CTA stops its chain, waits (bounded) for its copies and
-// MMAs still in flight, frees its TMEM and records the timeout in the status.
+// Thread 0 issues every MMA and bulk copy and is the only thread that waits
+// on their mbarriers (a spin on mbarrier.test_wait, bounded by ~1 s of SM
+// clock); the other threads meet it at the next CTA barrier instead of
+// polling.  An expired wait sets an abort flag, the CTA stops its chain,
+// thread 0 waits (bounded) for the copies and MMAs still in flight, the CTA
+// frees its TMEM and the timeout is recorded in the status.
 #pragma once
 
 namespace bss {
 
-constexpr int C64_R_BYTES = 65536;
-constexpr int C64_VR_BYTES = 2 * Geo<float, 64>::SLOT * 4;  // sS + sV = 34816
+constexpr int C64_LBO = 144;                    // next core matrix along K
+constexpr int C64_PART = 16 * C64_LBO;          // the lo part of a row group: 2304
+constexpr int C64_SBO = 2 * C64_PART;           // next 8-row group: 4608
+constexpr int C64_UPPER = 8 * C64_SBO;          // rows 64-127: 36864
+constexpr int C64_R_BYTES = 16 * C64_SBO;       // 73728
+constexpr int C64_VR_BYTES = 8 * C64_SBO;       // 36864 >= sS + sV (34816), >= a raw FP64 block (32768)
 constexpr int C64_THREADS = 256;
+constexpr long long C64_WAIT_CYCLES = 2000000000LL;  // ~1 s of SM clock
 
 constexpr size_t chain64_tc_smem() { return (size_t)C64_R_BYTES + C64_VR_BYTES + 256 + 64; }
 
 __device__ __forceinline__ uint32_t c64_off(int row, int k, int part)
 {
-    return (uint32_t)((row >> 3) * 4096 + part * 2048 + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4);
+    return (uint32_t)((row >> 3) * C64_SBO + part * C64_PART + (k >> 2) * C64_LBO + (row & 7) * 16 + (k & 3) * 4);
 }
 
 __device__ __forceinline__ uint64_t c64_desc(uint32_t saddr)
 {
     uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)(128u >> 4) << 16;   // leading byte offset: next core matrix along K
-    d |= (uint64_t)(4096u >> 4) << 32;  // stride byte offset: next 8-row group
-    d |= (uint64_t)1 << 46;             // descriptor version of the sm_100 family
+    d |= (uint64_t)(C64_LBO >> 4) << 16;  // leading byte offset: next core matrix along K
+    d |= (uint64_t)(C64_SBO >> 4) << 32;  // stride byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;               // descriptor version of the sm_100 family
     return d;
 }
 
@@ -77,9 +89,9 @@ __device__ __forceinline__ void c64_mma(uint32_t tm, uint32_t a, uint32_t b, boo
     constexpr uint32_t id = c64_idesc();
 #pragma unroll
     for (int kk = 0; kk < 8; ++kk) {
-        const uint32_t o = (uint32_t)kk * 256u;  // K = 8: two core matrices along K
-        const uint64_t ah = c64_desc(a + o), al = c64_desc(a + 2048u + o);
-        const uint64_t bh = c64_desc(b + o), bl = c64_desc(b + 2048u + o);
+        const uint32_t o = (uint32_t)kk * (2u * C64_LBO);  // K = 8: two core matrices along K
+        const uint64_t ah = c64_desc(a + o), al = c64_desc(a + C64_PART + o);
+        const uint64_t bh = c64_desc(b + o), bl = c64_desc(b + C64_PART + o);
         tc_mma(tm, ah, bh, id, (accumulate || kk) ? 1u : 0u);
         tc_mma(tm, ah, bl, id, 1u);
         tc_mma(tm, al, bh, id, 1u);
@@ -133,22 +145,42 @@ __device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
 
-// an outstanding mbarrier phase: wait for it (bounded); on expiry set the
-// abort flag and leave the phase outstanding (drained before exit)
+// an mbarrier and the parity of its outstanding phase (thread 0's view)
 struct C64Bar {
     uint32_t addr;
     uint32_t phase;
     bool pending;
 };
 
-__device__ __forceinline__ void c64_wait(C64Bar &b, int *abort)
+__device__ __forceinline__ bool mbar_test(uint32_t mbar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// thread 0 only: wait for the outstanding phase, at most C64_WAIT_CYCLES; on
+// expiry set the abort flag and leave the phase outstanding (drained before
+// exit).  The other threads learn the outcome at the next CTA barrier.
+__device__ __forceinline__ void c64_wait1(C64Bar &b, int *abort)
 {
     if (!b.pending) return;
-    if (mbar_wait(b.addr, b.phase)) {
-        b.phase ^= 1u;
-        b.pending = false;
-    } else {
-        *abort = 1;
+    const long long t0 = clock64();
+    for (;;) {
+        if (mbar_test(b.addr, b.phase)) {
+            b.phase ^= 1u;
+            b.pending = false;
+            return;
+        }
+        if (clock64() - t0 > C64_WAIT_CYCLES) {
+            *abort = 1;
+            return;
+        }
     }
 }
 
@@ -168,7 +200,7 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
     int *abort = reinterpret_cast<int *>(tail + 8);
     uint64_t *mbars = reinterpret_cast<uint64_t *>(tail + 16);  // MMA, A copy, B copy
     const Tin *rawA = reinterpret_cast<const Tin *>(VR);
-    const Tin *rawB = reinterpret_cast<const Tin *>(R + 32768);
+    const Tin *rawB = reinterpret_cast<const Tin *>(R + C64_UPPER);
 
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     const int L = 32 * (w & 3) + lane;  // this thread's TMEM lane (accumulator row)
@@ -203,43 +235,41 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
     const uint32_t sRa = smem_u32(R), sVa = smem_u32(VR);
     C64Bar bM{smem_u32(&mbars[0]), 0u, false}, bA{smem_u32(&mbars[1]), 0u, false}, bB{smem_u32(&mbars[2]), 0u, false};
 
-    if (first <= last && bulk) {
-        if (tid == 0) {
-            mbar_expect_tx(bA.addr, blk_bytes);
-            bulk_g2s(sVa, g.A_in + first * nn, blk_bytes, bA.addr);
-            bulk_prefetch_l2(g.B_in + first * nn, blk_bytes);
-        }
+    if (first <= last && bulk && tid == 0) {
+        mbar_expect_tx(bA.addr, blk_bytes);
+        bulk_g2s(sVa, g.A_in + first * nn, blk_bytes, bA.addr);
         bA.pending = true;
+        bulk_prefetch_l2(g.B_in + first * nn, blk_bytes);
     }
     bool sll_started = false;
     for (long long i = first; i <= last; ++i) {
         const long long t = i - first;
-        // ---- P1 and P3 on [W_{i-1} | Y_{i-1}] (written and fenced by the previous step)
-        if (t > 0) {
-            if (tid == 0) {
+        if (tid == 0) {
+            // ---- P1 and P3 on [W_{i-1} | Y_{i-1}] (written and fenced by the previous step)
+            if (t > 0) {
                 tc_fence_after();
                 c64_mma(tm, sRa, sRa, false);
-                c64_mma(tm + 64u, sRa, sRa + 32768u, sll_started);
+                c64_mma(tm + 64u, sRa, sRa + (uint32_t)C64_UPPER, sll_started);
                 tc_commit(bM.addr);
+                bM.pending = true;
+                sll_started = true;
             }
-            bM.pending = true;
-            sll_started = true;
+            c64_wait1(bM, abort);
+            // R has been read: B_i raw into its upper half (it lands during the Cholesky)
+            if (bulk) {
+                fence_async_smem();
+                mbar_expect_tx(bB.addr, blk_bytes);
+                bulk_g2s(sRa + (uint32_t)C64_UPPER, g.B_in + i * nn, blk_bytes, bB.addr);
+                bB.pending = true;
+            }
+            c64_wait1(bA, abort);
         }
         if (tid == 32 && bulk && i < last) {  // the next step's blocks into L2
             bulk_prefetch_l2(g.A_in + (i + 1) * nn, blk_bytes);
             bulk_prefetch_l2(g.B_in + (i + 1) * nn, blk_bytes);
         }
-        c64_wait(bM, abort);
-        // R has been read: B_i raw into its upper half (it lands during the Cholesky)
-        if (bulk) {
-            if (tid == 0) {
-                fence_async_smem();
-                mbar_expect_tx(bB.addr, blk_bytes);
-                bulk_g2s(sRa + 32768u, g.B_in + i * nn, blk_bytes, bB.addr);
-            }
-            bB.pending = true;
-        }
-        c64_wait(bA, abort);
+        __syncthreads();
+        if (*abort) break;
         tc_fence_after();
         // ---- Ahat_i (rows L < 64) and Z_i (rows L >= 64) from the P1 accumulator
         float dv[32];
@@ -289,59 +319,91 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
         }
         tc_fence_before();
         __syncthreads();
-        if (*abort) break;
         // ---- U^T U = Ahat, V = U^-1 (CUDA cores; ends with a CTA barrier)
         const int bad = chol_inv_blocked<float, 64, C64_THREADS>(sS, sV, dinv, sflag, tid);
         if (bad && tid == 0) record_bad_pivot(g.st, g.level, i);
-        // ---- V_i to HBM, and the V_i and B_i operands
-        c64_wait(bB, abort);
+        if (tid == 0) c64_wait1(bB, abort);
+        __syncthreads();
+        if (*abort) break;
+        // ---- V_i to HBM, and the V_i and B_i operands.  Thread (jr + 16 m, k4):
+        // 16 threads walk one column's 64 rows in float4 steps (conflict-free
+        // reads of the padded sV and of the raw block, coalesced V stores), and
+        // their operand writes land in distinct bank groups (leading byte offset 144)
         {
-            const int j = tid >> 2, k0 = (tid & 3) * 16;
-            float vv[16], bv[16];
+            const int jr = tid >> 4, k4 = (tid & 15) * 4;
+            float vv[4][4], bv[4][4];
             const Tin *Bg = g.B_in + i * nn;
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int k = k0 + q;
-                vv[q] = ((k >> 4) > (j >> 4)) ? 0.f : sV[k + j * LD];  // V's lower tiles are zero
-                bv[q] = (j < n && k < n) ? (float)(bulk ? rawB[k + j * n] : Bg[k + (long long)j * n]) : 0.f;
+            for (int m = 0; m < 4; ++m) {
+                const int j = jr + 16 * m;
+                const float4 v4 = *reinterpret_cast<const float4 *>(sV + k4 + j * LD);
+                const bool lower = (k4 >> 4) > (j >> 4);  // V's lower tiles are zero
+                vv[m][0] = lower ? 0.f : v4.x;
+                vv[m][1] = lower ? 0.f : v4.y;
+                vv[m][2] = lower ? 0.f : v4.z;
+                vv[m][3] = lower ? 0.f : v4.w;
+                if (bulk && n == 64) {  // 16-byte reads of the raw column
+                    if constexpr (sizeof(Tin) == 8) {
+                        const double2 b0 = *reinterpret_cast<const double2 *>(rawB + k4 + j * 64);
+                        const double2 b1 = *reinterpret_cast<const double2 *>(rawB + k4 + 2 + j * 64);
+                        bv[m][0] = (float)b0.x;
+                        bv[m][1] = (float)b0.y;
+                        bv[m][2] = (float)b1.x;
+                        bv[m][3] = (float)b1.y;
+                    } else {
+                        const float4 b4 = *reinterpret_cast<const float4 *>(rawB + k4 + j * 64);
+                        bv[m][0] = b4.x;
+                        bv[m][1] = b4.y;
+                        bv[m][2] = b4.z;
+                        bv[m][3] = b4.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int k = k4 + u;
+                        bv[m][u] = (j < n && k < n) ? (float)(bulk ? rawB[k + j * n] : Bg[k + (long long)j * n]) : 0.f;
+                    }
+                }
             }
             float *Vg = g.A_f + i * nn;
-            if (n == 64) {
 #pragma unroll
-                for (int q = 0; q < 16; q += 4)
-                    *reinterpret_cast<float4 *>(Vg + j * 64 + k0 + q) = make_float4(vv[q], vv[q + 1], vv[q + 2], vv[q + 3]);
-            } else if (j < n) {
+            for (int m = 0; m < 4; ++m) {
+                const int j = jr + 16 * m;
+                if (n == 64) {
+                    *reinterpret_cast<float4 *>(Vg + j * 64 + k4) = make_float4(vv[m][0], vv[m][1], vv[m][2], vv[m][3]);
+                } else if (j < n) {
 #pragma unroll
-                for (int q = 0; q < 16; ++q)
-                    if (k0 + q < n) Vg[(long long)j * n + k0 + q] = vv[q];
+                    for (int u = 0; u < 4; ++u)
+                        if (k4 + u < n) Vg[(long long)j * n + k4 + u] = vv[m][u];
+                }
             }
             __syncthreads();  // sV and the raw B_i are read: their bytes become operands
 #pragma unroll
-            for (int q = 0; q < 16; q += 4) {
-                c64_put4(VR, j, k0 + q, vv[q], vv[q + 1], vv[q + 2], vv[q + 3]);
-                c64_put4(R, 64 + j, k0 + q, bv[q], bv[q + 1], bv[q + 2], bv[q + 3]);
+            for (int m = 0; m < 4; ++m) {
+                const int j = jr + 16 * m;
+                c64_put4(VR, j, k4, vv[m][0], vv[m][1], vv[m][2], vv[m][3]);
+                c64_put4(R, 64 + j, k4, bv[m][0], bv[m][1], bv[m][2], bv[m][3]);
             }
         }
         fence_async_smem();
         __syncthreads();
-        if (*abort) break;
         // ---- P2 = [Z_i | B_i]^T V_i
         if (tid == 0) {
             tc_fence_after();
             c64_mma(tm, sRa, sVa, false);
             tc_commit(bM.addr);
-        }
-        bM.pending = true;
-        c64_wait(bM, abort);
-        tc_fence_after();
-        if (bulk && i < last) {  // V has been read: the next A block into VR
-            if (tid == 0) {
+            bM.pending = true;
+            c64_wait1(bM, abort);
+            if (bulk && i < last) {  // V has been read: the next A block into VR
                 fence_async_smem();
                 mbar_expect_tx(bA.addr, blk_bytes);
                 bulk_g2s(sVa, g.A_in + (i + 1) * nn, blk_bytes, bA.addr);
+                bA.pending = true;
             }
-            bA.pending = true;
         }
+        __syncthreads();
+        if (*abort) break;
+        tc_fence_after();
         // ---- Y_i (rows L < 64) and W_i (rows L >= 64): to HBM and into R as [W_i | Y_i]
         c64_ld32(tm + lane_base + (uint32_t)c0, dv);
         {
@@ -364,7 +426,6 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
-        if (*abort) break;
     }
 
     // ---- chain end: S_RR = W^T W, S_LR = Y^T W (P1) and the last S_LL term (P3)
@@ -372,11 +433,12 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
         if (tid == 0) {
             tc_fence_after();
             c64_mma(tm, sRa, sRa, false);
-            c64_mma(tm + 64u, sRa, sRa + 32768u, sll_started);
+            c64_mma(tm + 64u, sRa, sRa + (uint32_t)C64_UPPER, sll_started);
             tc_commit(bM.addr);
+            bM.pending = true;
+            c64_wait1(bM, abort);
         }
-        bM.pending = true;
-        c64_wait(bM, abort);
+        __syncthreads();
         tc_fence_after();
         float dv[32];
         float *Cp = g.C + p * 3 * nn;
@@ -399,13 +461,14 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
         }
     }
     __syncthreads();
-    if (*abort) {
+    if (*abort && tid == 0) {
         // a wait gave up: wait (bounded) for this CTA's copies and MMAs still
         // in flight before its shared memory and TMEM are released
-        if (bM.pending) mbar_wait(bM.addr, bM.phase);
-        if (bA.pending) mbar_wait(bA.addr, bA.phase);
-        if (bB.pending) mbar_wait(bB.addr, bB.phase);
-        if (tid == 0 && g.st) atomicExch(&g.st->tc_timeout, 1);
+        int ignored = 0;
+        c64_wait1(bM, &ignored);
+        c64_wait1(bA, &ignored);
+        c64_wait1(bB, &ignored);
+        if (g.st) atomicExch(&g.st->tc_timeout, 1);
     }
     tc_fence_before();
     __syncthreads();
