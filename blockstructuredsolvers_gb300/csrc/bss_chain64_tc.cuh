@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
         tc_fence_before();
         __syncthreads();
         // ---- U^T U = Ahat, V = U^-1 (CUDA cores; ends with a CTA barrier)
-        const int bad = chol_inv_blocked<float, 64, C64_THREADS>(sS, sV, dinv, sflag, tid);
+        const int bad = chol_inv_blocked<float, 64, C64_THREADS, true>(sS, sV, dinv, sflag, tid);
         if (bad && tid == 0) record_bad_pivot(g.st, g.level, i);
         if (tid == 0) c64_wait1(bB, abort);
         __syncthreads();

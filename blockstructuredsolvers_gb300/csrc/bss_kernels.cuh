@@ -320,7 +320,7 @@ struct Panel {
 };
 
 template <class T, int LD, int PB>
-__device__ __noinline__ int warp_chol(T *sS, T *dinv, int o, int lane)
+__device__ __forceinline__ int warp_chol_i(T *sS, T *dinv, int o, int lane)
 {
     const int r = lane & (PB - 1);
     T u[PB];
@@ -355,10 +355,15 @@ __device__ __noinline__ int warp_chol(T *sS, T *dinv, int o, int lane)
     }
     return bad;
 }
+template <class T, int LD, int PB>
+__device__ __noinline__ int warp_chol(T *sS, T *dinv, int o, int lane)
+{
+    return warp_chol_i<T, LD, PB>(sS, dinv, o, lane);
+}
 
 // V_KK = U_KK^{-1}: lane r computes column r by back substitution.
 template <class T, int LD, int PB>
-__device__ __noinline__ void warp_inv(const T *sS, const T *dinv, T *sV, int o, int lane)
+__device__ __forceinline__ void warp_inv_i(const T *sS, const T *dinv, T *sV, int o, int lane)
 {
     const int r = lane & (PB - 1);
     T v[PB];
@@ -379,10 +384,15 @@ __device__ __noinline__ void warp_inv(const T *sS, const T *dinv, T *sV, int o, 
         for (int c = 0; c < PB; ++c) sV[(o + c) + (o + r) * LD] = v[c];
     }
 }
+template <class T, int LD, int PB>
+__device__ __noinline__ void warp_inv(const T *sS, const T *dinv, T *sV, int o, int lane)
+{
+    warp_inv_i<T, LD, PB>(sS, dinv, sV, o, lane);
+}
 
 // row panel right of diagonal tile o: U(o:o+PB, c) = U_KK^{-T} S(o:o+PB, c)
 template <class T, int LD, int NB, int PB>
-__device__ __noinline__ void panel_trsm(T *sS, const T *dinv, int o, int t0, int nthr)
+__device__ __forceinline__ void panel_trsm_i(T *sS, const T *dinv, int o, int t0, int nthr)
 {
     for (int c = o + PB + t0; c < NB; c += nthr) {
         T x[PB];
@@ -398,10 +408,15 @@ __device__ __noinline__ void panel_trsm(T *sS, const T *dinv, int o, int t0, int
         for (int p = 0; p < PB; ++p) sS[(o + p) + c * LD] = x[p];
     }
 }
+template <class T, int LD, int NB, int PB>
+__device__ __noinline__ void panel_trsm(T *sS, const T *dinv, int o, int t0, int nthr)
+{
+    panel_trsm_i<T, LD, NB, PB>(sS, dinv, o, t0, nthr);
+}
 
 // S(a, b) -= sum_p U(o+p, a) U(o+p, b)   for o+PB <= a <= b < NB
 template <class T, int LD, int NB, int PB>
-__device__ __noinline__ void trailing_update(T *sS, int o, int tid, int nthr)
+__device__ __forceinline__ void trailing_update_i(T *sS, int o, int tid, int nthr)
 {
     using V = typename Vec<T>::type;
     constexpr int W = Vec<T>::W;
@@ -420,6 +435,11 @@ __device__ __noinline__ void trailing_update(T *sS, int o, int tid, int nthr)
         }
         sS[ca + cb * LD] -= acc;
     }
+}
+template <class T, int LD, int NB, int PB>
+__device__ __noinline__ void trailing_update(T *sS, int o, int tid, int nthr)
+{
+    trailing_update_i<T, LD, NB, PB>(sS, o, tid, nthr);
 }
 
 // off-diagonal tiles of V = U^{-1} after the factorization (FP64 chains):
@@ -474,7 +494,7 @@ __device__ __noinline__ void inverse_stages(T *sS, T *sV, int tid, int nthr)
 // being factored.  One thread per row (I, a): the 16 sums T(a, :) in
 // registers, then the row of -T V_JJ.
 template <class T, int LD, int PB>
-__device__ __noinline__ void inv_column(const T *sS, T *sV, int J, int t0, int nthr)
+__device__ __forceinline__ void inv_column_i(const T *sS, T *sV, int J, int t0, int nthr)
 {
     for (int e = t0; e < J * PB; e += nthr) {
         const int I = e / PB, a = e - I * PB;
@@ -500,6 +520,11 @@ __device__ __noinline__ void inv_column(const T *sS, T *sV, int J, int t0, int n
         }
     }
 }
+template <class T, int LD, int PB>
+__device__ __noinline__ void inv_column(const T *sS, T *sV, int J, int t0, int nthr)
+{
+    inv_column_i<T, LD, PB>(sS, sV, J, t0, nthr);
+}
 
 // Factor the tile in sS into sV = U^{-1}.  Returns nonzero (in every thread)
 // if a pivot failed.  Ends with a __syncthreads.  Per panel K: warp 0
@@ -507,7 +532,10 @@ __device__ __noinline__ void inv_column(const T *sS, T *sV, int J, int t0, int n
 // column K-1; then warp 1 inverts the diagonal tile while the rest solve the
 // row panel; then the trailing update.  V's last block column follows the
 // loop (FP32); FP64 forms V's off-diagonal tiles in stages after it.
-template <class T, int NB, int THREADS>
+// INL: the panel helpers are inlined into the caller (no call saves and
+// restores of the caller's registers on the critical warp); the default
+// calls them out of line, which keeps register-heavy callers from spilling
+template <class T, int NB, int THREADS, bool INL = false>
 __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sflag, int tid)
 {
     static_assert(THREADS > 32, "two warps at least");
@@ -520,25 +548,48 @@ __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sfla
     for (int K = 0; K < KP; ++K) {
         const int o = PB * K;
         if (warp == 0) {
-            const int bad = warp_chol<T, LD, PB>(sS, dinv, o, lane);
+            int bad;
+            if constexpr (INL)
+                bad = warp_chol_i<T, LD, PB>(sS, dinv, o, lane);
+            else
+                bad = warp_chol<T, LD, PB>(sS, dinv, o, lane);
             if (bad && lane == 0) *sflag = 1;
         } else if (K >= 2 && sizeof(T) == 4) {
-            inv_column<T, LD, PB>(sS, sV, K - 1, tid - 32, THREADS - 32);
+            if constexpr (INL)
+                inv_column_i<T, LD, PB>(sS, sV, K - 1, tid - 32, THREADS - 32);
+            else
+                inv_column<T, LD, PB>(sS, sV, K - 1, tid - 32, THREADS - 32);
         }
         __syncthreads();
-        if (warp == 1) warp_inv<T, LD, PB>(sS, dinv, sV, o, lane);
+        if (warp == 1) {
+            if constexpr (INL)
+                warp_inv_i<T, LD, PB>(sS, dinv, sV, o, lane);
+            else
+                warp_inv<T, LD, PB>(sS, dinv, sV, o, lane);
+        }
         if (K + 1 < KP) {
             const int t0 = warp == 0 ? lane : tid - 32;
-            if (warp != 1) panel_trsm<T, LD, NB, PB>(sS, dinv, o, t0, THREADS - 32);
+            if (warp != 1) {
+                if constexpr (INL)
+                    panel_trsm_i<T, LD, NB, PB>(sS, dinv, o, t0, THREADS - 32);
+                else
+                    panel_trsm<T, LD, NB, PB>(sS, dinv, o, t0, THREADS - 32);
+            }
             __syncthreads();
-            trailing_update<T, LD, NB, PB>(sS, o, tid, THREADS);
+            if constexpr (INL)
+                trailing_update_i<T, LD, NB, PB>(sS, o, tid, THREADS);
+            else
+                trailing_update<T, LD, NB, PB>(sS, o, tid, THREADS);
         }
         __syncthreads();
     }
     if constexpr (sizeof(T) == 8) {
         inverse_stages<T, LD, NB, PB>(sS, sV, tid, THREADS);
     } else if (KP > 1) {
-        inv_column<T, LD, PB>(sS, sV, KP - 1, tid, THREADS);
+        if constexpr (INL)
+            inv_column_i<T, LD, PB>(sS, sV, KP - 1, tid, THREADS);
+        else
+            inv_column<T, LD, PB>(sS, sV, KP - 1, tid, THREADS);
         __syncthreads();
     }
     return *sflag;
@@ -646,7 +697,7 @@ __device__ __forceinline__ void chain_factor_body(const ChainFactorArgs<Tin, T> 
         store_tile_smem<T, NB>(sS, S, ti, tj, T(1));
         if (has_next) store_tile_smem<T, NB>(sB, Bi, ti, tj, T(1));
         __syncthreads();
-        const int bad = chol_inv_blocked<T, NB, TL::THREADS>(sS, sV, dinv, sflag, tid);
+        const int bad = chol_inv_blocked<T, NB, TL::THREADS, NB == 64>(sS, sV, dinv, sflag, tid);
         if (bad && tid == 0) record_bad_pivot(g.st, g.level, i);
 
         T accY[TL::RA][TL::RB], accW[TL::RA][TL::RB];
