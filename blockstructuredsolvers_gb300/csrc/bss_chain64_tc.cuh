@@ -18,7 +18,7 @@
 // cholesky_factorize_batched! and the Schur products of
 // compute_schur_complement! (src/backbone_cuda.jl:70-101, 143-157).
 //
-// Shared memory (108.3 KB: two CTAs per SM):
+// Shared memory (108.6 KB: two CTAs per SM):
 //   R   72 KB  the stacked A operand in the no-swizzle K-major layout of
 //              8-row x 16-byte core matrices, with the hi and lo parts
 //              interleaved per 8-row group: element (row, k) of part h at
@@ -60,7 +60,7 @@ constexpr int C64_VR_BYTES = 8 * C64_SBO;       // 36864 >= sS + sV (34816), >= 
 constexpr int C64_THREADS = 256;
 constexpr long long C64_WAIT_CYCLES = 2000000000LL;  // ~1 s of SM clock
 
-constexpr size_t chain64_tc_smem() { return (size_t)C64_R_BYTES + C64_VR_BYTES + 256 + 64; }
+constexpr size_t chain64_tc_smem() { return (size_t)C64_R_BYTES + C64_VR_BYTES + 512 + 64; }
 
 __device__ __forceinline__ uint32_t c64_off(int row, int k, int part)
 {
@@ -194,7 +194,8 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
     float *sS = reinterpret_cast<float *>(VR);
     float *sV = sS + Geo<float, 64>::SLOT;
     float *dinv = reinterpret_cast<float *>(VR + C64_VR_BYTES);
-    unsigned char *tail = VR + C64_VR_BYTES + 256;
+    float *prow = dinv + 64;  // 64 floats: the Cholesky's pivot-row buffer
+    unsigned char *tail = VR + C64_VR_BYTES + 512;
     int *sflag = reinterpret_cast<int *>(tail);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(tail + 4);
     int *abort = reinterpret_cast<int *>(tail + 8);
@@ -320,7 +321,7 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
         tc_fence_before();
         __syncthreads();
         // ---- U^T U = Ahat, V = U^-1 (CUDA cores; ends with a CTA barrier)
-        const int bad = chol_inv_blocked<float, 64, C64_THREADS, true>(sS, sV, dinv, sflag, tid);
+        const int bad = chol_inv_blocked<float, 64, C64_THREADS, true, true>(sS, sV, dinv, sflag, tid, prow);
         if (bad && tid == 0) record_bad_pivot(g.st, g.level, i);
         if (tid == 0) c64_wait1(bB, abort);
         __syncthreads();

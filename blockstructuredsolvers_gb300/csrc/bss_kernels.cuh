@@ -526,6 +526,151 @@ __device__ __noinline__ void inv_column(const T *sS, T *sV, int J, int t0, int n
     inv_column_i<T, LD, PB>(sS, sV, J, t0, nthr);
 }
 
+// ---- FP32 forms of the panel steps for callers with registers to spare ------
+// Measured on GB300 (one 64 x 64 tile, 256 threads, alone on an SM): the
+// 16-wide pivot chain took ~3.1K cycles with one shuffle per broadcast
+// element and ~2.5K with the pivot row broadcast through shared memory; the
+// first panel's trailing update ~2.6K with one 16-term dot per loop trip and
+// ~1.8K register-tiled; the last block column of V ~3.6K on 48 threads and
+// ~2.3K element-parallel on 256.  The whole factorization + inverse: 25.0K
+// -> 20.7K cycles.
+
+// 16-wide panel Cholesky by one warp (as warp_chol_i), the pivot row U(j, :)
+// broadcast through `row` (64 floats of shared memory, double-buffered): one
+// 32-lane store and four 128-bit broadcast reads per pivot instead of up to
+// 15 dependent shuffles
+template <int LD, int PB>
+__device__ __forceinline__ int warp_chol_row(float *sS, float *dinv, float *row, int o, int lane)
+{
+    const int r = lane & (PB - 1);
+    float u[PB];
+#pragma unroll
+    for (int c = 0; c < PB; ++c) u[c] = sS[(o + c) + (o + r) * LD];  // S(o+c, o+r), valid for c <= r
+    float diag = sS[(o + r) + (o + r) * LD];
+    int bad = 0;
+    float udiag = 1.f;
+#pragma unroll
+    for (int j = 0; j < PB; ++j) {
+        float piv = __shfl_sync(0xffffffffu, diag, j);
+        if (!(piv > 0.f && piv < INFINITY)) {
+            bad = 1;
+            piv = 1.f;
+        }
+        const float rs = rsqrtf(piv);
+        const float ujr = (r == j ? diag : u[j]) * rs;  // U(j, r) for r >= j
+        if (j == r) udiag = ujr;
+        diag = fmaf(-ujr, ujr, diag);  // own column's diagonal: the pivot chain
+        u[j] = ujr;
+        if (j + 1 < PB) {
+            float *rj = row + 32 * (j & 1);
+            if (lane < PB) rj[r] = ujr;
+            __syncwarp();
+#pragma unroll
+            for (int c4 = ((j + 1) / 4) * 4; c4 < PB; c4 += 4) {
+                const float4 v = *reinterpret_cast<const float4 *>(rj + c4);
+                const float ua[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    if (c4 + t > j) u[c4 + t] = fmaf(-ua[t], ujr, u[c4 + t]);  // S(c, r) -= U(j,c) U(j,r)
+            }
+        }
+    }
+    if (lane < PB) {
+#pragma unroll
+        for (int c = 0; c < PB; ++c)
+            if (c <= r) sS[(o + c) + (o + r) * LD] = (c == r) ? udiag : u[c];
+        dinv[o + r] = 1.f / udiag;
+    }
+    return bad;
+}
+
+// trailing update of panel o in FP32: S(a, b) -= sum_p U(o+p, a) U(o+p, b)
+// over the whole trailing block (the Cholesky reads only its upper
+// triangle): lanes take rows a (and a + 32), warps take columns b; a thread
+// keeps its U columns in registers and reads each U(., b) as a broadcast, all
+// in 128-bit steps (column reads conflict-free for LD = NB + 4)
+template <int LD, int NB, int PB, int THREADS>
+__device__ __forceinline__ void trailing_update_f32(float *sS, int o, int tid)
+{
+    static_assert(PB == 16, "four float4 per column segment");
+    constexpr int NW = THREADS / 32;
+    const int m = NB - o - PB, c0 = o + PB;
+    const int warp = tid >> 5, lane = tid & 31;
+    float4 ua[2][4];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int a = lane + 32 * h;
+        if (a < m) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) ua[h][q] = *reinterpret_cast<const float4 *>(sS + o + 4 * q + (c0 + a) * LD);
+        }
+    }
+    for (int b = warp; b < m; b += NW) {
+        float4 ub[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) ub[q] = *reinterpret_cast<const float4 *>(sS + o + 4 * q + (c0 + b) * LD);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int a = lane + 32 * h;
+            if (a < m) {
+                float acc = 0.f;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) fma_vec(acc, ua[h][q], ub[q]);
+                sS[(c0 + a) + (c0 + b) * LD] -= acc;
+            }
+        }
+    }
+}
+
+// Off-diagonal block column J of V = U^{-1} in FP32, element-parallel over
+// `nthr` threads from t0 in two stages (`bar` = the barrier joining exactly
+// those threads: 0 for the whole CTA, else a named barrier):
+//   T_IJ = sum_{P=I..J-1} V_IP U_PJ      kept in the scratch lower tile (J, I) of sS
+//   V_IJ = -T_IJ V_JJ
+// The lower tiles of sS are never read as matrix data (the Cholesky reads
+// the upper triangle), and (J, I) lies outside the diagonal tile being
+// factored while this runs.
+template <int LD, int PB>
+__device__ __forceinline__ void inv_column_par(float *sS, float *sV, int J, int t0, int nthr, int bar)
+{
+    const int total = J * PB * PB;
+    for (int e = t0; e < total; e += nthr) {
+        const int I = e / (PB * PB), w = e - I * PB * PB;
+        const int a = w % PB, c = w / PB;
+        float s0 = 0.f, s1 = 0.f;
+        for (int P = I; P < J; ++P)
+#pragma unroll
+            for (int q = 0; q < PB; q += 4) {
+                const float4 u = *reinterpret_cast<const float4 *>(sS + (PB * P + q) + (PB * J + c) * LD);  // U_PJ(q.., c)
+                const float *vr = sV + (PB * I + a) + (PB * P + q) * LD;                                   // V_IP(a, q..)
+                s0 = fmaf(vr[0], u.x, s0);
+                s1 = fmaf(vr[LD], u.y, s1);
+                s0 = fmaf(vr[2 * LD], u.z, s0);
+                s1 = fmaf(vr[3 * LD], u.w, s1);
+            }
+        sS[(PB * J + a) + (PB * I + c) * LD] = s0 + s1;
+    }
+    if (bar == 0)
+        __syncthreads();
+    else
+        asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthr) : "memory");
+    for (int e = t0; e < total; e += nthr) {
+        const int I = e / (PB * PB), w = e - I * PB * PB;
+        const int a = w % PB, b = w / PB;
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int c = 0; c < PB; c += 4) {
+            const float4 v = *reinterpret_cast<const float4 *>(sV + (PB * J + c) + (PB * J + b) * LD);  // V_JJ(c.., b)
+            const float *tr = sS + (PB * J + a) + (PB * I + c) * LD;                                   // T(a, c..)
+            s0 = fmaf(tr[0], v.x, s0);
+            s1 = fmaf(tr[LD], v.y, s1);
+            s0 = fmaf(tr[2 * LD], v.z, s0);
+            s1 = fmaf(tr[3 * LD], v.w, s1);
+        }
+        sV[(PB * I + a) + (PB * J + b) * LD] = -(s0 + s1);
+    }
+}
+
 // Factor the tile in sS into sV = U^{-1}.  Returns nonzero (in every thread)
 // if a pivot failed.  Ends with a __syncthreads.  Per panel K: warp 0
 // factors the diagonal tile while (FP32) the other warps form V's block
@@ -534,10 +679,14 @@ __device__ __noinline__ void inv_column(const T *sS, T *sV, int J, int t0, int n
 // loop (FP32); FP64 forms V's off-diagonal tiles in stages after it.
 // INL: the panel helpers are inlined into the caller (no call saves and
 // restores of the caller's registers on the critical warp); the default
-// calls them out of line, which keeps register-heavy callers from spilling
-template <class T, int NB, int THREADS, bool INL = false>
-__device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sflag, int tid)
+// calls them out of line, which keeps register-heavy callers from spilling.
+// FAST (FP32, with INL; `row` = 64 floats of shared memory): the FP32 forms
+// above; the named barrier 1 joins the THREADS - 32 threads that form V's
+// block columns during the panels.
+template <class T, int NB, int THREADS, bool INL = false, bool FAST = false>
+__device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sflag, int tid, T *row = nullptr)
 {
+    static_assert(!FAST || (INL && sizeof(T) == 4), "the fast forms are inlined FP32");
     static_assert(THREADS > 32, "two warps at least");
     constexpr int LD = Geo<T, NB>::LD;
     constexpr int PB = Panel<NB>::PB;
@@ -549,13 +698,17 @@ __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sfla
         const int o = PB * K;
         if (warp == 0) {
             int bad;
-            if constexpr (INL)
+            if constexpr (FAST)
+                bad = warp_chol_row<LD, PB>(sS, dinv, row, o, lane);
+            else if constexpr (INL)
                 bad = warp_chol_i<T, LD, PB>(sS, dinv, o, lane);
             else
                 bad = warp_chol<T, LD, PB>(sS, dinv, o, lane);
             if (bad && lane == 0) *sflag = 1;
         } else if (K >= 2 && sizeof(T) == 4) {
-            if constexpr (INL)
+            if constexpr (FAST)
+                inv_column_par<LD, PB>(sS, sV, K - 1, tid - 32, THREADS - 32, 1);
+            else if constexpr (INL)
                 inv_column_i<T, LD, PB>(sS, sV, K - 1, tid - 32, THREADS - 32);
             else
                 inv_column<T, LD, PB>(sS, sV, K - 1, tid - 32, THREADS - 32);
@@ -576,7 +729,9 @@ __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sfla
                     panel_trsm<T, LD, NB, PB>(sS, dinv, o, t0, THREADS - 32);
             }
             __syncthreads();
-            if constexpr (INL)
+            if constexpr (FAST)
+                trailing_update_f32<LD, NB, PB, THREADS>(sS, o, tid);
+            else if constexpr (INL)
                 trailing_update_i<T, LD, NB, PB>(sS, o, tid, THREADS);
             else
                 trailing_update<T, LD, NB, PB>(sS, o, tid, THREADS);
@@ -586,7 +741,9 @@ __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sfla
     if constexpr (sizeof(T) == 8) {
         inverse_stages<T, LD, NB, PB>(sS, sV, tid, THREADS);
     } else if (KP > 1) {
-        if constexpr (INL)
+        if constexpr (FAST)
+            inv_column_par<LD, PB>(sS, sV, KP - 1, tid, THREADS, 0);
+        else if constexpr (INL)
             inv_column_i<T, LD, PB>(sS, sV, KP - 1, tid, THREADS);
         else
             inv_column<T, LD, PB>(sS, sV, KP - 1, tid, THREADS);
