@@ -1133,7 +1133,7 @@ def roofline_chain_factor(bss, A, B, d, hbm_gbs, peak_kind):
             "note": "latency-bound chain: the HBM fraction is low by construction"}
 
 
-TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "chain_factor_mixed_N4096_n64.md")
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "chain64_tc_mixed_N4096_n64.md")
 KERNEL_SOURCES = [os.path.join(ROOT, "blockstructuredsolvers_gb300", "csrc", f)
                   for f in ("bss_kernels.cuh", "bss_tc.cuh", "bss_chain64_tc.cuh")]
 
