@@ -664,6 +664,7 @@ SolveArgs<T> bss::make_solve_args(bss_handle *h, int l, int j0, int kc)
     a.j0 = j0;
     a.kc = kc;
     a.seq = L.seq ? 1 : 0;
+    a.st = h->st;
     return a;
 }
 template SolveArgs<double> bss::make_solve_args<double>(bss_handle *, int, int, int);
@@ -964,7 +965,8 @@ extern "C" int bss_synchronize(bss_handle *h)
         h->sticky = h->h_st->done ? BSS_OK : BSS_ERR_NOT_CONVERGED;
     }
     if (h->factored && h->h_st->tc_timeout)
-        return fail(BSS_ERR_TIMEOUT, "a bounded tensor-core wait expired during factorize; the factors are void");
+        return fail(BSS_ERR_TIMEOUT, "a bounded device wait expired (tensor-core factorization or streamed solve); "
+                                     "the result is void");
     const unsigned long long key = h->h_st->bad_key;
     if (h->factored && key != ~0ULL) {
         h->info.failed_level = (int32_t)(key >> 40);

@@ -1756,6 +1756,7 @@ struct SolveArgs {
     int j0;        // first column of this pass
     int kc;        // columns in this pass
     int seq;
+    DevStatus *st; // a bounded wait of the streamed sweeps records its expiry here
 };
 
 // shared memory: 2 buffers x 3 blocks (staged form only) + 6 vectors +
@@ -2891,3 +2892,4 @@ __global__ void init_identity_kernel(T *A, long long first_blk, long long last_b
 }  // namespace bss
 
 #include "bss_chain64_tc.cuh"
+#include "bss_stream.cuh"

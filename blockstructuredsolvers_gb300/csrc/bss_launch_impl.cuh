@@ -143,9 +143,26 @@ static cudaError_t set_solve_smem(const void *kern, size_t smem)
     return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
+// the streamed sweeps need 16-byte aligned blocks and right-hand sides
+template <class T>
+static bool stream_aligned(const SolveArgs<T> &a)
+{
+    const uintptr_t m = (uintptr_t)a.Af | (uintptr_t)a.Bf | (uintptr_t)a.Y | (uintptr_t)a.d;
+    return (m & 15u) == 0 && ((size_t)a.n * sizeof(T)) % 16 == 0;
+}
+
 template <class T>
 cudaError_t launch_chain_fwd(const SolveArgs<T> &a, cudaStream_t s)
 {
+    if (!a.seq && solve_streamed<T>(a.n, a.kc) && stream_aligned(a)) {
+        const size_t smem = stream_smem_bytes<T>(a.n, a.kc);
+        auto kern = chain_fwd_stream_kernel<T>;
+        cudaError_t e = set_solve_smem<T>((const void *)kern, smem);
+        if (e != cudaSuccess) return e;
+        kern<<<(unsigned)a.Q, SOLVE_THREADS, smem, s>>>(a);
+        count_launch();
+        return cudaGetLastError();
+    }
     const bool staged = solve_staged<T>(a.n, a.kc);
     const size_t smem = solve_smem_bytes<T>(a.n, a.kc, staged);
     auto kern = staged ? chain_fwd_kernel<T, true> : chain_fwd_kernel<T, false>;
@@ -160,6 +177,15 @@ cudaError_t launch_chain_fwd(const SolveArgs<T> &a, cudaStream_t s)
 template <class T, class Tsep>
 cudaError_t launch_chain_bwd(const SolveArgs<T> &a, cudaStream_t s)
 {
+    if (solve_streamed<T>(a.n, a.kc) && stream_aligned(a)) {
+        const size_t smem = stream_smem_bytes<T>(a.n, a.kc);
+        auto kern = chain_bwd_stream_kernel<T, Tsep>;
+        cudaError_t e = set_solve_smem<T>((const void *)kern, smem);
+        if (e != cudaSuccess) return e;
+        kern<<<(unsigned)a.Q, SOLVE_THREADS, smem, s>>>(a);
+        count_launch();
+        return cudaGetLastError();
+    }
     const bool staged = solve_staged<T>(a.n, a.kc);
     const size_t smem = solve_smem_bytes<T>(a.n, a.kc, staged);
     auto kern = staged ? chain_bwd_kernel<T, Tsep, true> : chain_bwd_kernel<T, Tsep, false>;

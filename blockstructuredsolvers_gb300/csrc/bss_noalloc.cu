@@ -185,6 +185,7 @@ int run(long long N, int n, int k, T *A, T *B, T *d, cudaStream_t s)
             a.j0 = j0;
             a.kc = kc;
             a.seq = lv[l].seq ? 1 : 0;
+            a.st = st;
             NA_CHECK(launch_chain_fwd<T>(a, s));
             if (!lv[l].seq)
                 NA_CHECK((launch_assemble_rhs<T, T>((const T *)lv[l].d, (const T *)lv[l].bvec, (T *)lv[l + 1].d,
@@ -205,6 +206,7 @@ int run(long long N, int n, int k, T *A, T *B, T *d, cudaStream_t s)
             a.j0 = j0;
             a.kc = kc;
             a.seq = 0;
+            a.st = st;
             NA_CHECK((launch_chain_bwd<T, T>(a, s)));
         }
     }
