@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "libbss_gb300.so")
 
 BSS_OK = 0
 BSS_FACTOR_FMA_CHAIN = 1
+BSS_FACTOR_WIDE_L2 = 2
 BSS_ERR_ARG = 1
 BSS_ERR_OOM = 2
 BSS_ERR_CUDA = 3

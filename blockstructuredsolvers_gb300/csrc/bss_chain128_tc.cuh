@@ -1,0 +1,476 @@
+// Chain factor kernel for wide blocks (n in 65..128) with FP32 factors on the
+// 5th-generation tensor cores, one CTA per SM: one CTA walks one partition's
+// chain like chain_factor_body (same recursion, same outputs V_i, W_i, Y_i
+// and S_LL / S_RR / S_LR), holding the whole step on chip.  Reference: the
+// potrf/trsm/gemm sequence of cholesky_factorize_batched! and the Schur
+// products of compute_schur_complement! (src/backbone_cuda.jl:70-101,
+// 143-157).
+//
+// Products (3xTF32: x = hi + lo, C = Xh Yh + Xh Yl + Xl Yh in the FP32 TMEM
+// accumulator, relative error ~2^-21 like FP32 FMA products), each an
+// M = 128, N = 128 MMA sequence D(m, j) = sum_k A(m, k) B(j, k) over K = 128
+// in chunks of 16.  "op(X)" is the operand whose row m is column m of X:
+//   phase 1 (from the carried W_{i-1}, Y_{i-1}):
+//     D1 = op(W) op(W)^T = W^T W          -> Ahat_i = A_i - W^T W
+//     D2 = op(Y) op(W)^T = Y^T W = -Z_i^T  (row m of D2 is -column m of Z_i)
+//     S_LL += op(Y) op(Y)^T = Y^T Y        (accumulated in TMEM over the chain)
+//   phase 2 (after U^T U = Ahat_i, V_i = U^-1 on the CUDA cores):
+//     D1 = op(Z) op(V)^T = Z^T V = Y_i^T   (row m of D1 is column m of Y_i)
+//     DW = op(B) op(V)^T = B^T V = W_i^T
+// and at the chain end phase 1 on the last W, Y gives S_RR = W^T W (D1),
+// S_LR = Y^T W (D2) and the last S_LL term.  A row of a Y_i^T / W_i^T
+// accumulator is a row of the next step's operand, so the factors never
+// leave the chip between the step that makes them and the step that uses
+// them; they are written to HBM once, for the solve.
+//
+// Tensor memory (512 columns, 128 lanes): S_LL | D1 | D2 | DW, 128 columns each.
+//
+// Shared memory (~197 KB):
+//   [0, 66 KB)      the carried Y_{i-1} as op(Y) rows (FP32, row stride 132
+//                   floats) during phase 1; then V (sV, the Cholesky's
+//                   column-major tile, leading dimension 132)
+//   [66, 132 KB)    the carried W_{i-1} rows during phase 1; then Ahat / U
+//                   (sS); then, with the next 30 KB, the two phase-2 stages
+//   [132, 196 KB)   the two phase-1 stages
+//   control words   pivot reciprocals, pivot-row buffer, flags, TMEM
+//                   address, two mbarriers
+// A stage holds one K = 16 chunk of each operand it feeds, split into hi and
+// lo TF32 parts, each part 128 rows x 16 K in the canonical no-swizzle
+// K-major layout: 8-row x 16-byte core matrices, the four of a row group
+// adjacent along K (leading byte offset 128), row groups 512 bytes apart
+// (stride byte offset 512).  Converter threads take consecutive rows, so
+// each quarter-warp reads and writes 128 contiguous bytes: no bank
+// conflicts.  The chunk after the one being multiplied is split while the
+// tensor core works on the current one.
+//
+// Block loads: A_i is read by the Ahat readout and B_i by the phase-2
+// converters straight from L2, where both were prefetched
+// (cp.async.bulk.prefetch.L2) a whole step ahead; each thread issues all of
+// its loads of a block before using any.
+//
+// Thread 0 issues every MMA and is the only thread that waits on the
+// mbarriers (a spin on mbarrier.test_wait bounded by ~1 s of SM clock); the
+// others meet it at the next CTA barrier.  An expired wait sets an abort
+// flag, the CTA stops its chain, thread 0 waits (bounded) for the MMAs still
+// in flight, the CTA frees its TMEM and the timeout is recorded in the status.
+#pragma once
+
+namespace bss {
+
+constexpr int C128_THREADS = 256;
+constexpr int C128_LD = Geo<float, 128>::LD;              // 132
+constexpr int C128_RLD = 132;                             // row stride of the carried operands (floats)
+constexpr int C128_MAT = 128 * C128_LD * 4;               // 67584: one padded 128 x 128 FP32 matrix
+constexpr int C128_PART = 128 * 16 * 4;                   // 8192: one split part of a K = 16 chunk
+constexpr int C128_STAGE1 = 4 * C128_PART;                // W hi, W lo, Y hi, Y lo
+constexpr int C128_STAGE2 = 6 * C128_PART;                // Z hi, Z lo, B hi, B lo, V hi, V lo
+constexpr int C128_OFF_Y = 0;                             // carried Y / sV
+constexpr int C128_OFF_X = C128_MAT;                      // carried W / sS / phase-2 stages
+constexpr int C128_OFF_S1 = 2 * C128_MAT;                 // phase-1 stages
+constexpr int C128_OFF_CTL = C128_OFF_S1 + 2 * C128_STAGE1;
+constexpr int C128_NCHUNK = 8;                            // K = 128 in chunks of 16
+constexpr uint32_t C128_T_SLL = 0, C128_T_D1 = 128, C128_T_D2 = 256, C128_T_DW = 384;  // TMEM columns
+static_assert(C128_OFF_X + 2 * C128_STAGE2 <= C128_OFF_CTL, "phase-2 stages fit below the control words");
+
+constexpr size_t chain128_tc_smem() { return (size_t)C128_OFF_CTL + 1024; }
+
+// byte offset of (row m, K group k4 .. k4+3) in one part of a stage
+__device__ __forceinline__ uint32_t c128_off(int m, int k4)
+{
+    return (uint32_t)((m >> 3) * 512 + (k4 >> 2) * 128 + (m & 7) * 16);
+}
+
+__device__ __forceinline__ uint64_t c128_desc(uint32_t saddr)
+{
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)(128u >> 4) << 16;  // leading byte offset: next core matrix along K
+    d |= (uint64_t)(512u >> 4) << 32;  // stride byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;            // descriptor version of the sm_100 family
+    return d;
+}
+
+// TMEM cols at tm (+)= A x B^T over one K = 16 chunk in 3xTF32 (parts at
+// shared addresses ah/al, bh/bl); issued by one thread
+__device__ __forceinline__ void c128_mma16(uint32_t tm, uint32_t ah, uint32_t al, uint32_t bh, uint32_t bl,
+                                           bool accumulate)
+{
+    constexpr uint32_t id = tc_idesc_128x128();
+#pragma unroll
+    for (int kk = 0; kk < 2; ++kk) {
+        const uint32_t o = (uint32_t)kk * 256u;  // K = 8: two core matrices along K
+        tc_mma(tm, c128_desc(ah + o), c128_desc(bh + o), id, (accumulate || kk) ? 1u : 0u);
+        tc_mma(tm, c128_desc(ah + o), c128_desc(bl + o), id, 1u);
+        tc_mma(tm, c128_desc(al + o), c128_desc(bh + o), id, 1u);
+    }
+}
+
+// four values split into hi / lo TF32 parts, stored at part offset o
+__device__ __forceinline__ void c128_put4(unsigned char *hi, unsigned char *lo, uint32_t o, float a, float b, float c,
+                                          float d)
+{
+    const uint32_t h0 = to_tf32(a), h1 = to_tf32(b), h2 = to_tf32(c), h3 = to_tf32(d);
+    *reinterpret_cast<uint4 *>(hi + o) = make_uint4(h0, h1, h2, h3);
+    *reinterpret_cast<uint4 *>(lo + o) =
+        make_uint4(to_tf32(a - __uint_as_float(h0)), to_tf32(b - __uint_as_float(h1)),
+                   to_tf32(c - __uint_as_float(h2)), to_tf32(d - __uint_as_float(h3)));
+}
+
+// 8 consecutive accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void c128_ld8(uint32_t addr, float (&v)[8])
+{
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(addr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+// column-major n x n block from the carried rows (row m = column m)
+__device__ __forceinline__ void c128_store_block(float *dst, const float *raw, int n, int tid)
+{
+    if (n == 128) {
+        for (int e = tid; e < 128 * 32; e += C128_THREADS) {
+            const int m = e >> 5, k4 = (e & 31) * 4;
+            *reinterpret_cast<float4 *>(dst + m * 128 + k4) = *reinterpret_cast<const float4 *>(raw + m * C128_RLD + k4);
+        }
+    } else {
+        for (int e = tid; e < n * n; e += C128_THREADS) {
+            const int m = e / n, k = e - m * n;
+            dst[e] = raw[m * C128_RLD + k];
+        }
+    }
+}
+
+// thread 0: wait for both stages' last commits
+__device__ __forceinline__ void c128_drain(C64Bar (&bar)[2], int *abort)
+{
+    c64_wait1(bar[0], abort);
+    c64_wait1(bar[1], abort);
+}
+
+// phase 1 on the carried rows: D1 = W^T W, D2 = Y^T W, S_LL (+)= Y^T Y.
+// Returns false (in every thread) when a wait expired; on return the
+// products are complete in TMEM.
+__device__ __forceinline__ bool c128_phase1(uint32_t tm, const float *rawW, const float *rawY, unsigned char *stages,
+                                            uint32_t stages_addr, C64Bar (&bar)[2], int *abort, bool sll, int tid)
+{
+    const int rm = tid & 127, rq = tid >> 7;
+#pragma unroll 1
+    for (int c = 0; c < C128_NCHUNK; ++c) {
+        const int s = c & 1;
+        if (tid == 0) c64_wait1(bar[s], abort);  // the MMAs that last read stage s are done
+        tc_fence_before();
+        __syncthreads();
+        if (*abort) return false;
+        unsigned char *st = stages + s * C128_STAGE1;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int q = rq + 2 * h;
+            const uint32_t o = c128_off(rm, 4 * q);
+            const float4 wv = *reinterpret_cast<const float4 *>(rawW + rm * C128_RLD + 16 * c + 4 * q);
+            const float4 yv = *reinterpret_cast<const float4 *>(rawY + rm * C128_RLD + 16 * c + 4 * q);
+            c128_put4(st, st + C128_PART, o, wv.x, wv.y, wv.z, wv.w);
+            c128_put4(st + 2 * C128_PART, st + 3 * C128_PART, o, yv.x, yv.y, yv.z, yv.w);
+        }
+        fence_async_smem();  // generic-proxy stores -> visible to the tensor core
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t a = stages_addr + (uint32_t)(s * C128_STAGE1);
+            const uint32_t wh = a, wl = a + C128_PART, yh = a + 2 * C128_PART, yl = a + 3 * C128_PART;
+            c128_mma16(tm + C128_T_D1, wh, wl, wh, wl, c > 0);
+            c128_mma16(tm + C128_T_D2, yh, yl, wh, wl, c > 0);
+            c128_mma16(tm + C128_T_SLL, yh, yl, yh, yl, sll || c > 0);
+            tc_commit(bar[s].addr);
+            bar[s].pending = true;
+        }
+    }
+    if (tid == 0) c128_drain(bar, abort);
+    __syncthreads();
+    tc_fence_after();
+    return *abort == 0;
+}
+
+template <class Tin>
+__global__ void __launch_bounds__(C128_THREADS, 1) chain128_tc_kernel(ChainFactorArgs<Tin, float> g)
+{
+    constexpr int LD = C128_LD;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *rawY = reinterpret_cast<float *>(smem_raw + C128_OFF_Y);
+    float *sV = rawY;
+    float *rawW = reinterpret_cast<float *>(smem_raw + C128_OFF_X);
+    float *sS = rawW;
+    unsigned char *ctl = smem_raw + C128_OFF_CTL;
+    float *dinv = reinterpret_cast<float *>(ctl);  // 128 pivot reciprocals
+    float *prow = dinv + 128;                      // 64 floats: the Cholesky's pivot-row buffer
+    int *sflag = reinterpret_cast<int *>(ctl + 768);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(ctl + 772);
+    int *abort = reinterpret_cast<int *>(ctl + 776);
+    uint64_t *mbars = reinterpret_cast<uint64_t *>(ctl + 784);  // stage 0, stage 1
+
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int L = 32 * (w & 3) + lane;  // this thread's TMEM lane (accumulator row)
+    const int cb = 64 * (w >> 2);       // its first accumulator column
+    const uint32_t lane_base = (uint32_t)(32 * (w & 3)) << 16;
+    const int rm = tid & 127, rq = tid >> 7;  // converter mapping: operand row, K group
+    const int n = g.n;
+    const long long nn = (long long)n * n;
+    const uint32_t blk_bytes = (uint32_t)(nn * (long long)sizeof(Tin));
+    const bool pf = (blk_bytes % 16u) == 0 && ((uintptr_t)g.A_in % 16u) == 0 && ((uintptr_t)g.B_in % 16u) == 0;
+
+    if (w == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"(512u)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int q = 0; q < 2; ++q)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbars[q])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *abort = 0;
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tm = *tslot;
+    const uint32_t base_addr = smem_u32(smem_raw);
+    C64Bar bar[2] = {{smem_u32(&mbars[0]), 0u, false}, {smem_u32(&mbars[1]), 0u, false}};
+
+    // partitions p = blockIdx.x, + gridDim.x, ... (the grid is at most one CTA per SM)
+    for (long long p = blockIdx.x; p < g.Q && !*abort; p += gridDim.x) {
+    const long long sL = (p * (g.N - 1)) / g.Q;
+    const long long sR = ((p + 1) * (g.N - 1)) / g.Q;
+    const long long first = sL + 1, last = sR - 1;
+    if (tid == 0 && pf && first <= last) {
+        bulk_prefetch_l2(g.A_in + first * nn, blk_bytes);
+        bulk_prefetch_l2(g.B_in + first * nn, blk_bytes);
+        bulk_prefetch_l2(g.B_in + sL * nn, blk_bytes);
+    }
+    bool sll = false;
+    for (long long i = first; i <= last; ++i) {
+        const long long t = i - first;
+        if (tid == 32 && pf && i < last) {  // the next step's blocks into L2
+            bulk_prefetch_l2(g.A_in + (i + 1) * nn, blk_bytes);
+            bulk_prefetch_l2(g.B_in + (i + 1) * nn, blk_bytes);
+        }
+        // ---- phase 1: D1 = W^T W, D2 = Y^T W, S_LL += Y^T Y on the carried rows
+        if (t > 0) {
+            if (!c128_phase1(tm, rawW, rawY, smem_raw + C128_OFF_S1, base_addr + C128_OFF_S1, bar, abort, sll, tid))
+                break;
+            sll = true;
+        }
+        // ---- Ahat_i = A_i - D1 into sS (identity outside n x n); sS overlays the carried W, read by now
+        {
+            const Tin *Ag = g.A_in + i * nn;
+#pragma unroll 1
+            for (int hf = 0; hf < 2; ++hf) {
+                const int c0 = cb + 32 * hf;
+                // every load is issued (clamped to a valid address) before any is
+                // used, so a thread has its 32 loads in flight at once
+                Tin ga[32];
+#pragma unroll
+                for (int q = 0; q < 32; ++q) {
+                    const int c = c0 + q;
+                    ga[q] = __ldcg(Ag + ((L < n && c < n) ? L + (long long)c * n : 0));
+                }
+                float a[32];
+#pragma unroll
+                for (int q = 0; q < 32; ++q) {
+                    const int c = c0 + q;
+                    a[q] = (L < n && c < n) ? (float)ga[q] : (L == c ? 1.f : 0.f);
+                }
+                float d[32];
+                if (t > 0) {
+                    c64_ld32(tm + lane_base + C128_T_D1 + (uint32_t)c0, d);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 32; ++q) d[q] = 0.f;
+                }
+#pragma unroll
+                for (int q = 0; q < 32; ++q) sS[L + (c0 + q) * LD] = (L < n && c0 + q < n) ? a[q] - d[q] : a[q];
+            }
+        }
+        __syncthreads();
+        // ---- U^T U = Ahat, V = U^-1 (CUDA cores; ends with a CTA barrier)
+        const int bad = chol_inv_blocked<float, 128, C128_THREADS, true, true>(sS, sV, dinv, sflag, tid, prow);
+        if (bad && tid == 0) record_bad_pivot(g.st, g.level, i);
+        // ---- phase 2: D1 = Z^T V = Y_i^T, DW = B^T V = W_i^T; V_i to HBM on the way
+        {
+            // this thread's B_i values of every chunk: column rm, rows 16 c + 8 rq .. +7,
+            // all loads issued before any is used (clamped addresses; 16-byte
+            // loads through L1 when n = 128, which keep each sector's second
+            // half for the next load)
+            float bv[C128_NCHUNK][8];
+            const Tin *Bg = g.B_in + i * nn;
+            if (n == 128) {
+                using V2 = typename Vec<Tin>::type;
+                constexpr int W2 = Vec<Tin>::W;
+                V2 gb[C128_NCHUNK][8 / W2];
+#pragma unroll
+                for (int c = 0; c < C128_NCHUNK; ++c)
+#pragma unroll
+                    for (int u = 0; u < 8 / W2; ++u)
+                        gb[c][u] = __ldg(reinterpret_cast<const V2 *>(Bg + 16 * c + 8 * rq + W2 * u + rm * 128));
+#pragma unroll
+                for (int c = 0; c < C128_NCHUNK; ++c)
+#pragma unroll
+                    for (int u = 0; u < 8 / W2; ++u) {
+                        if constexpr (W2 == 2) {
+                            bv[c][2 * u] = (float)gb[c][u].x;
+                            bv[c][2 * u + 1] = (float)gb[c][u].y;
+                        } else {
+                            bv[c][4 * u] = gb[c][u].x;
+                            bv[c][4 * u + 1] = gb[c][u].y;
+                            bv[c][4 * u + 2] = gb[c][u].z;
+                            bv[c][4 * u + 3] = gb[c][u].w;
+                        }
+                    }
+            } else {
+                Tin gb[C128_NCHUNK][8];
+#pragma unroll
+                for (int c = 0; c < C128_NCHUNK; ++c)
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int k = 16 * c + 8 * rq + u;
+                        gb[c][u] = __ldg(Bg + ((rm < n && k < n) ? k + (long long)rm * n : 0));
+                    }
+#pragma unroll
+                for (int c = 0; c < C128_NCHUNK; ++c)
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int k = 16 * c + 8 * rq + u;
+                        bv[c][u] = (rm < n && k < n) ? (float)gb[c][u] : 0.f;
+                    }
+            }
+            const Tin *Bs = g.B_in + sL * nn;  // Z_first = B_sL^T
+            float *Vg = g.A_f + i * nn;
+#pragma unroll
+            for (int c = 0; c < C128_NCHUNK; ++c) {
+                const int s = c & 1;
+                if (tid == 0) c64_wait1(bar[s], abort);
+                tc_fence_before();
+                __syncthreads();
+                if (*abort) break;
+                unsigned char *st = smem_raw + C128_OFF_X + s * C128_STAGE2;
+                // V: op(V) row m = column m of V (zero below the diagonal tiles)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int q = rq + 2 * h, k = 16 * c + 4 * q;
+                    float4 v = *reinterpret_cast<const float4 *>(sV + k + rm * LD);
+                    if ((k >> 4) > (rm >> 4)) v = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (n == 128) {
+                        *reinterpret_cast<float4 *>(Vg + k + rm * 128) = v;
+                    } else if (rm < n) {
+                        const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            if (k + u < n) Vg[k + u + (long long)rm * n] = vv[u];
+                    }
+                    c128_put4(st + 4 * C128_PART, st + 5 * C128_PART, c128_off(rm, 4 * q), v.x, v.y, v.z, v.w);
+                }
+                // B: op(B) row m = column m of B_i
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    c128_put4(st + 2 * C128_PART, st + 3 * C128_PART, c128_off(rm, 8 * rq + 4 * h), bv[c][4 * h],
+                              bv[c][4 * h + 1], bv[c][4 * h + 2], bv[c][4 * h + 3]);
+                // Z: op(Z) row m = column m of Z_i = -(row m of D2); Z_first = B_sL^T
+                {
+                    const int kz = 8 * (w >> 2);
+                    float z[8];
+                    if (t > 0) {
+                        c128_ld8(tm + lane_base + C128_T_D2 + (uint32_t)(16 * c + kz), z);
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) z[u] = -z[u];
+                    } else {
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const int k = 16 * c + kz + u;
+                            z[u] = (L < n && k < n) ? (float)__ldcg(Bs + L + (long long)k * n) : 0.f;
+                        }
+                    }
+                    c128_put4(st, st + C128_PART, c128_off(L, kz), z[0], z[1], z[2], z[3]);
+                    c128_put4(st, st + C128_PART, c128_off(L, kz + 4), z[4], z[5], z[6], z[7]);
+                }
+                fence_async_smem();
+                __syncthreads();
+                if (tid == 0) {
+                    tc_fence_after();
+                    const uint32_t a = base_addr + C128_OFF_X + (uint32_t)(s * C128_STAGE2);
+                    const uint32_t zh = a, zl = a + C128_PART, bh = a + 2 * C128_PART, bl = a + 3 * C128_PART;
+                    const uint32_t vh = a + 4 * C128_PART, vl = a + 5 * C128_PART;
+                    c128_mma16(tm + C128_T_D1, zh, zl, vh, vl, c > 0);
+                    c128_mma16(tm + C128_T_DW, bh, bl, vh, vl, c > 0);
+                    tc_commit(bar[s].addr);
+                    bar[s].pending = true;
+                }
+            }
+        }
+        if (tid == 0) c128_drain(bar, abort);
+        __syncthreads();
+        if (*abort) break;
+        tc_fence_after();
+        // ---- Y_i, W_i: TMEM rows -> carried rows (next step's operands) -> HBM
+#pragma unroll 1
+        for (int hf = 0; hf < 2; ++hf) {
+            const int c0 = cb + 32 * hf;
+            float d[32];
+            c64_ld32(tm + lane_base + C128_T_D1 + (uint32_t)c0, d);
+#pragma unroll
+            for (int q = 0; q < 32; q += 4)
+                *reinterpret_cast<float4 *>(rawY + L * C128_RLD + c0 + q) = make_float4(d[q], d[q + 1], d[q + 2], d[q + 3]);
+            c64_ld32(tm + lane_base + C128_T_DW + (uint32_t)c0, d);
+#pragma unroll
+            for (int q = 0; q < 32; q += 4)
+                *reinterpret_cast<float4 *>(rawW + L * C128_RLD + c0 + q) = make_float4(d[q], d[q + 1], d[q + 2], d[q + 3]);
+        }
+        __syncthreads();
+        c128_store_block(g.Y + i * nn, rawY, n, tid);
+        c128_store_block(g.B_f + i * nn, rawW, n, tid);
+    }
+
+    // ---- chain end: S_RR = W^T W (D1), S_LR = Y^T W (D2), S_LL += Y^T Y
+    if (!*abort && first <= last) {
+        if (c128_phase1(tm, rawW, rawY, smem_raw + C128_OFF_S1, base_addr + C128_OFF_S1, bar, abort, sll, tid)) {
+            float *Cp = g.C + p * 3 * nn;
+#pragma unroll 1
+            for (int hf = 0; hf < 2; ++hf) {
+                const int c0 = cb + 32 * hf;
+#pragma unroll 1
+                for (int r = 0; r < 3; ++r) {  // S_LL, S_RR, S_LR
+                    const uint32_t col = r == 0 ? C128_T_SLL : (r == 1 ? C128_T_D1 : C128_T_D2);
+                    float d[32];
+                    c64_ld32(tm + lane_base + col + (uint32_t)c0, d);
+                    float *dst = Cp + r * nn;
+                    if (L < n) {
+#pragma unroll
+                        for (int q = 0; q < 32; ++q)
+                            if (c0 + q < n) dst[L + (long long)(c0 + q) * n] = d[q];
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    }  // partitions
+    __syncthreads();
+    if (*abort && tid == 0) {
+        // a wait gave up: wait (bounded) for this CTA's MMAs still in flight
+        // before its shared memory and TMEM are released
+        int ignored = 0;
+        c64_wait1(bar[0], &ignored);
+        c64_wait1(bar[1], &ignored);
+        if (g.st) atomicExch(&g.st->tc_timeout, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (w == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(512u) : "memory");
+    }
+}
+
+}  // namespace bss

@@ -252,8 +252,8 @@ extern "C" int bss_diag_fma_peak(int32_t dtype, double *tflops)
 
 extern "C" int bss_diag_set_factor_variant(int32_t variant)
 {
-    if (variant < 0 || variant > FACTOR_FMA_CHAIN)
-        return fail(BSS_ERR_ARG, "bss_diag_set_factor_variant: 0 or BSS_FACTOR_FMA_CHAIN");
+    if (variant < 0 || (variant & ~FACTOR_VARIANTS) != 0)
+        return fail(BSS_ERR_ARG, "bss_diag_set_factor_variant: a combination of BSS_FACTOR_FMA_CHAIN, BSS_FACTOR_WIDE_L2");
     set_default_factor_variant(variant);
     return BSS_OK;
 }

@@ -586,7 +586,7 @@ __device__ __forceinline__ int warp_chol_row(float *sS, float *dinv, float *row,
 
 // trailing update of panel o in FP32: S(a, b) -= sum_p U(o+p, a) U(o+p, b)
 // over the whole trailing block (the Cholesky reads only its upper
-// triangle): lanes take rows a (and a + 32), warps take columns b; a thread
+// triangle): lanes take rows a (a + 32, ... up to the tile), warps take columns b; a thread
 // keeps its U columns in registers and reads each U(., b) as a broadcast, all
 // in 128-bit steps (column reads conflict-free for LD = NB + 4)
 template <int LD, int NB, int PB, int THREADS>
@@ -594,11 +594,12 @@ __device__ __forceinline__ void trailing_update_f32(float *sS, int o, int tid)
 {
     static_assert(PB == 16, "four float4 per column segment");
     constexpr int NW = THREADS / 32;
+    constexpr int H = (NB - PB + 31) / 32;  // row groups of 32 per lane
     const int m = NB - o - PB, c0 = o + PB;
     const int warp = tid >> 5, lane = tid & 31;
-    float4 ua[2][4];
+    float4 ua[H][4];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < H; ++h) {
         const int a = lane + 32 * h;
         if (a < m) {
 #pragma unroll
@@ -610,7 +611,7 @@ __device__ __forceinline__ void trailing_update_f32(float *sS, int o, int tid)
 #pragma unroll
         for (int q = 0; q < 4; ++q) ub[q] = *reinterpret_cast<const float4 *>(sS + o + 4 * q + (c0 + b) * LD);
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < H; ++h) {
             const int a = lane + 32 * h;
             if (a < m) {
                 float acc = 0.f;
@@ -776,6 +777,8 @@ struct ChainFactorArgs {
 // chosen per handle (the defaults, or the autotuner's choice per (n, dtype))
 enum {
     FACTOR_FMA_CHAIN = 1,  // 33 <= n <= 64, FP32 factors: CUDA-core chain kernel instead of the tensor-core one
+    FACTOR_WIDE_L2 = 2,    // 65 <= n <= 128, FP32 factors: the L2-staged wide kernel instead of chain128_tc
+    FACTOR_VARIANTS = 3,   // every bit
 };
 
 template <class T, int NB>
@@ -2892,4 +2895,5 @@ __global__ void init_identity_kernel(T *A, long long first_blk, long long last_b
 }  // namespace bss
 
 #include "bss_chain64_tc.cuh"
+#include "bss_chain128_tc.cuh"
 #include "bss_stream.cuh"

@@ -58,10 +58,37 @@ static cudaError_t wide_chain_factor_tc(const ChainFactorArgs<Tin, T> &a, cudaSt
     return cudaGetLastError();
 }
 
+// partitioned levels of 65..128-wide blocks with FP32 factors: the chain
+// kernel that keeps a step on chip (bss_chain128_tc.cuh), unless the
+// L2-staged wide kernel is chosen
+template <class Tin>
+static bool use_chain128(const ChainFactorArgs<Tin, float> &a)
+{
+    return !a.seq && a.n <= 128 && !(a.variant & FACTOR_WIDE_L2);
+}
+
+template <class Tin>
+static cudaError_t chain128_tc(const ChainFactorArgs<Tin, float> &a, cudaStream_t s)
+{
+    const size_t smem = chain128_tc_smem();
+    auto kern = chain128_tc_kernel<Tin>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned grid = (unsigned)(a.Q < sms ? a.Q : sms);  // one CTA per SM walks several partitions
+    kern<<<grid, C128_THREADS, smem, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
 template <class Tin, class T>
 static cudaError_t wide_chain_factor(const ChainFactorArgs<Tin, T> &a, cudaStream_t s)
 {
     if constexpr (std::is_same<T, float>::value) {
+        if (use_chain128<Tin>(a)) return chain128_tc<Tin>(a, s);
         if (wide_uses_tc<T>(a.n)) return wide_chain_factor_tc<Tin, T, true>(a, s);
     }
     return wide_chain_factor_tc<Tin, T, false>(a, s);
@@ -120,6 +147,10 @@ int chain_factor_ctas_per_sm(int n, int variant)
     case 64: return ctas_nb<Tin, T, 64>(variant);
     case WIDE_CLASS:
         if constexpr (std::is_same<T, float>::value) {
+            // the on-chip kernel runs one CTA per SM over several partitions
+            // each; the partitions are sized for the level's solve sweeps,
+            // which run two CTAs per SM
+            if (n <= 128 && !(variant & FACTOR_WIDE_L2)) return 2;
             if (wide_uses_tc<T>(n)) return wide_ctas_tc<Tin, T, true>();
         }
         return wide_ctas_tc<Tin, T, false>();

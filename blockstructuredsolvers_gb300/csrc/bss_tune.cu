@@ -194,9 +194,11 @@ extern "C" int bss_autotune(int64_t n, int32_t dtype, int32_t precision, int64_t
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int t0 = precision == BSS_PRECISION_MIXED ? BSS_F32 : dtype;
-    // kernel variants worth timing: FP32 factors of 33..64-wide blocks have two chain kernels
+    // kernel variants worth timing: FP32 factors of 33..64-wide and of
+    // 65..128-wide blocks have two chain kernels each
     std::vector<int> variants{0};
     if (t0 == BSS_F32 && tile_for((int)n) == 64) variants = {0, FACTOR_FMA_CHAIN};
+    if (t0 == BSS_F32 && tile_for((int)n) == WIDE_CLASS && n <= 128) variants = {0, FACTOR_WIDE_L2};
     // candidates run with the process-wide default variant set to theirs and
     // no table entry for this key (the default is restored afterwards)
     const int saved_default = default_factor_variant();
@@ -312,7 +314,7 @@ extern "C" int bss_autotune_load(const char *path)
                                     &e.factor_variant);
         if (got == 8) e.factor_variant = 0;
         if ((got == 8 || got == 9) && e.n > 0 && e.wave_mult_x4 > 0 && e.seq_cutoff > 0 && e.chain_blocks > 0 &&
-            e.factor_variant >= 0 && e.factor_variant <= FACTOR_FMA_CHAIN) {
+            e.factor_variant >= 0 && (e.factor_variant & ~FACTOR_VARIANTS) == 0) {
             g_tune[std::make_tuple(e.n, e.dtype, e.precision)] = e;
             ++loaded;
         }

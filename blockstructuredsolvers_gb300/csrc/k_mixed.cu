@@ -45,7 +45,7 @@ cudaError_t launch_relres_control(DevStatus *st, double tol, int max_refine, cud
 
 static std::atomic<int> g_factor_variant{0};
 int default_factor_variant() { return g_factor_variant.load(std::memory_order_relaxed); }
-void set_default_factor_variant(int v) { g_factor_variant.store(v & FACTOR_FMA_CHAIN); }
+void set_default_factor_variant(int v) { g_factor_variant.store(v & FACTOR_VARIANTS); }
 
 int tile_for(int n)
 {

@@ -448,8 +448,13 @@ int bss_diag_fma_peak(int32_t dtype, double *tflops);
  * 3xTF32 products, bulk-copied block tiles).  A handle takes the autotuner's
  * variant for its (n, dtype, precision) when there is one, else the
  * process-wide default set here (0 at start).  Applies to handles and
- * batches created after the call. */
+ * batches created after the call.  BSS_FACTOR_WIDE_L2: partitioned levels
+ * of 65 <= n <= 128 blocks with FP32 factors run on the wide kernel whose
+ * tensor-core operands are re-staged from L2 per product (two CTAs per SM)
+ * instead of the kernel that keeps a chain step on chip (one CTA per SM,
+ * factors carried in shared and tensor memory between steps). */
 #define BSS_FACTOR_FMA_CHAIN 1
+#define BSS_FACTOR_WIDE_L2 2
 int bss_diag_set_factor_variant(int32_t variant);
 int32_t bss_diag_get_factor_variant(void);
 
