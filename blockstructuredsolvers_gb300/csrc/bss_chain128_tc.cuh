@@ -25,15 +25,18 @@
 //
 // Tensor memory (512 columns, 128 lanes): S_LL | D1 | D2 | DW, 128 columns each.
 //
-// Shared memory (~197 KB):
+// Shared memory (~217 KB), by phase of a step:
 //   [0, 66 KB)      the carried Y_{i-1} as op(Y) rows (FP32, row stride 132
-//                   floats) during phase 1; then V (sV, the Cholesky's
-//                   column-major tile, leading dimension 132)
-//   [66, 132 KB)    the carried W_{i-1} rows during phase 1; then Ahat / U
+//                   floats) in phase 1; A_i column chunks 1-4 for the Ahat
+//                   readout; then V (sV, the Cholesky's column-major tile,
+//                   leading dimension 132)
+//   [66, 132 KB)    the carried W_{i-1} rows in phase 1; then Ahat / U
 //                   (sS); then, with the next 30 KB, the two phase-2 stages
-//   [132, 196 KB)   the two phase-1 stages
+//   [132, 196 KB)   the two phase-1 stages; A_i chunks 5-7; the B_i chunks
+//   [196, 216 KB)   A_i chunk 0 (lands during phase 1); the third B_i chunk
 //   control words   pivot reciprocals, pivot-row buffer, flags, TMEM
-//                   address, two mbarriers
+//                   address, mbarriers (two stages, eight A chunks, three
+//                   B chunks)
 // A stage holds one K = 16 chunk of each operand it feeds, split into hi and
 // lo TF32 parts, each part 128 rows x 16 K in the canonical no-swizzle
 // K-major layout: 8-row x 16-byte core matrices, the four of a row group
@@ -43,10 +46,20 @@
 // conflicts.  The chunk after the one being multiplied is split while the
 // tensor core works on the current one.
 //
-// Block loads: A_i is read by the Ahat readout and B_i by the phase-2
-// converters straight from L2, where both were prefetched
-// (cp.async.bulk.prefetch.L2) a whole step ahead; each thread issues all of
-// its loads of a block before using any.
+// Block loads are bulk copies (cp.async.bulk) completing on mbarriers, and
+// both blocks are hinted into L2 (cp.async.bulk.prefetch.L2) a step ahead:
+// A_i in column chunks of 16 (contiguous in the column-major block), chunk 0
+// issued at the step's start into a buffer of its own, the others as soon
+// as phase 1 has released their buffers; B_i in row chunks of 16 (the K
+// chunks of op(B)): one 2D tensor copy per chunk (cp.async.bulk.tensor, box
+// of 16 rows x 128 columns of the level's B, out-of-range rows and columns
+// filled with zeros) with the 128-byte swizzle, so that the converters'
+// reads of eight consecutive columns hit eight different bank groups; three
+// chunks in flight: the first three land during the Cholesky, each later
+// one is issued when the chunk three before it has been split (FP64 input,
+// the first level of the mixed path; FP32 levels read B_i with plain loads).
+// Blocks whose columns do not start on 16 bytes (odd n; FP32 input with n
+// not a multiple of 4) are read with plain loads.
 //
 // Thread 0 issues every MMA and is the only thread that waits on the
 // mbarriers (a spin on mbarrier.test_wait bounded by ~1 s of SM clock); the
@@ -67,10 +80,62 @@ constexpr int C128_STAGE2 = 6 * C128_PART;                // Z hi, Z lo, B hi, B
 constexpr int C128_OFF_Y = 0;                             // carried Y / sV
 constexpr int C128_OFF_X = C128_MAT;                      // carried W / sS / phase-2 stages
 constexpr int C128_OFF_S1 = 2 * C128_MAT;                 // phase-1 stages
-constexpr int C128_OFF_CTL = C128_OFF_S1 + 2 * C128_STAGE1;
+constexpr int C128_ACH = 16 * 128 * 8;                   // one A_i column chunk (16 FP64 columns)
+constexpr int C128_BCH = 16 * 128 * 8;                   // one B_i row chunk: 128 columns x 16 rows (FP64)
+constexpr int C128_NBBUF = 3;                             // B_i chunks in flight
+constexpr int C128_OFF_B = C128_OFF_X + 2 * C128_STAGE2;  // B_i chunk buffers (Cholesky, phase 2)
+constexpr int C128_OFF_A0 = C128_OFF_S1 + 2 * C128_STAGE1;  // A_i chunk 0 (phase 1)
+constexpr int C128_OFF_CTL = C128_OFF_B + C128_NBBUF * C128_BCH > C128_OFF_A0 + C128_ACH
+                                 ? C128_OFF_B + C128_NBBUF * C128_BCH
+                                 : C128_OFF_A0 + C128_ACH;
 constexpr int C128_NCHUNK = 8;                            // K = 128 in chunks of 16
 constexpr uint32_t C128_T_SLL = 0, C128_T_D1 = 128, C128_T_D2 = 256, C128_T_DW = 384;  // TMEM columns
-static_assert(C128_OFF_X + 2 * C128_STAGE2 <= C128_OFF_CTL, "phase-2 stages fit below the control words");
+static_assert(C128_OFF_A0 + C128_ACH <= C128_OFF_CTL, "A chunk 0 below the control words");
+static_assert(C128_OFF_B % 1024 == 0 && C128_BCH % 1024 == 0, "128-byte-swizzled TMA boxes start on 1024 bytes");
+
+// byte offset of logical byte `off` of a box that the tensor copy wrote with
+// the 128-byte swizzle: the 16-byte unit index (bits 4-6) XOR the 128-byte
+// row index (bits 7-9)
+__device__ __forceinline__ uint32_t c128_swz(uint32_t off) { return off ^ (((off >> 7) & 7u) << 4); }
+
+// one 2D tensor copy (box of the tensor map at element coordinates x = row,
+// y = column) into shared memory, completing on the mbarrier
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t mbar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(mbar)
+        : "memory");
+}
+static_assert(4 * C128_ACH <= C128_MAT && C128_OFF_S1 + 3 * C128_ACH <= C128_OFF_S1 + 2 * C128_STAGE1,
+              "A chunks 1-7 fit the carried-Y region and the phase-1 stages");
+
+// shared-memory offset of A_i column chunk j: chunk 0 has a buffer of its
+// own (it lands while phase 1 still holds the other regions), chunks 1-4
+// take the carried-Y region and 5-7 the phase-1 stages once phase 1 is done
+__host__ __device__ constexpr int c128_achunk(int j)
+{
+    return j == 0 ? C128_OFF_A0 : (j <= 4 ? C128_OFF_Y + (j - 1) * C128_ACH : C128_OFF_S1 + (j - 5) * C128_ACH);
+}
+
+// thread 0: bounded wait on the mbarrier at `addr` whose outstanding parity
+// is bit j of `phase` when bit j of `pending` is set; sets *abort on expiry
+__device__ __forceinline__ void c128_waitbit(uint32_t addr, int j, uint32_t &phase, uint32_t &pending, int *abort)
+{
+    if (!((pending >> j) & 1u)) return;
+    const long long t0 = clock64();
+    for (;;) {
+        if (mbar_test(addr, (phase >> j) & 1u)) {
+            phase ^= 1u << j;
+            pending &= ~(1u << j);
+            return;
+        }
+        if (clock64() - t0 > C64_WAIT_CYCLES) {
+            *abort = 1;
+            return;
+        }
+    }
+}
 
 constexpr size_t chain128_tc_smem() { return (size_t)C128_OFF_CTL + 1024; }
 
@@ -151,10 +216,13 @@ __device__ __forceinline__ void c128_drain(C64Bar (&bar)[2], int *abort)
 }
 
 // phase 1 on the carried rows: D1 = W^T W, D2 = Y^T W, S_LL (+)= Y^T Y.
-// Returns false (in every thread) when a wait expired; on return the
-// products are complete in TMEM.
+// Thread 0 calls rows_read() once the last chunk is split (the carried rows
+// are free; the stages are not, until the drain).  Returns false (in every
+// thread) when a wait expired; on return the products are complete in TMEM.
+template <class F>
 __device__ __forceinline__ bool c128_phase1(uint32_t tm, const float *rawW, const float *rawY, unsigned char *stages,
-                                            uint32_t stages_addr, C64Bar (&bar)[2], int *abort, bool sll, int tid)
+                                            uint32_t stages_addr, C64Bar (&bar)[2], int *abort, bool sll, int tid,
+                                            F rows_read)
 {
     const int rm = tid & 127, rq = tid >> 7;
 #pragma unroll 1
@@ -185,6 +253,7 @@ __device__ __forceinline__ bool c128_phase1(uint32_t tm, const float *rawW, cons
             c128_mma16(tm + C128_T_SLL, yh, yl, yh, yl, sll || c > 0);
             tc_commit(bar[s].addr);
             bar[s].pending = true;
+            if (c == C128_NCHUNK - 1) rows_read();  // every carried row has been split
         }
     }
     if (tid == 0) c128_drain(bar, abort);
@@ -194,7 +263,8 @@ __device__ __forceinline__ bool c128_phase1(uint32_t tm, const float *rawW, cons
 }
 
 template <class Tin>
-__global__ void __launch_bounds__(C128_THREADS, 1) chain128_tc_kernel(ChainFactorArgs<Tin, float> g)
+__global__ void __launch_bounds__(C128_THREADS, 1)
+    chain128_tc_kernel(ChainFactorArgs<Tin, float> g, const __grid_constant__ CUtensorMap tmB, int tma_b)
 {
     constexpr int LD = C128_LD;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -208,7 +278,7 @@ __global__ void __launch_bounds__(C128_THREADS, 1) chain128_tc_kernel(ChainFacto
     int *sflag = reinterpret_cast<int *>(ctl + 768);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(ctl + 772);
     int *abort = reinterpret_cast<int *>(ctl + 776);
-    uint64_t *mbars = reinterpret_cast<uint64_t *>(ctl + 784);  // stage 0, stage 1
+    uint64_t *mbars = reinterpret_cast<uint64_t *>(ctl + 784);  // stages 0-1, A chunks 2-9, B chunks 10-12
 
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     const int L = 32 * (w & 3) + lane;  // this thread's TMEM lane (accumulator row)
@@ -218,7 +288,12 @@ __global__ void __launch_bounds__(C128_THREADS, 1) chain128_tc_kernel(ChainFacto
     const int n = g.n;
     const long long nn = (long long)n * n;
     const uint32_t blk_bytes = (uint32_t)(nn * (long long)sizeof(Tin));
-    const bool pf = (blk_bytes % 16u) == 0 && ((uintptr_t)g.A_in % 16u) == 0 && ((uintptr_t)g.B_in % 16u) == 0;
+    const bool aligned = ((uintptr_t)g.A_in % 16u) == 0 && ((uintptr_t)g.B_in % 16u) == 0;
+    const bool pf = (blk_bytes % 16u) == 0 && aligned;
+    // bulk copies of column chunks (A) and the tensor copies of row chunks (B)
+    // start on 16 bytes; the latter also need the 1024-byte-aligned buffers
+    const bool bulk = aligned && (sizeof(Tin) == 8 ? n % 2 == 0 : n % 4 == 0);
+    const bool tmab = sizeof(Tin) == 8 && bulk && tma_b != 0 && ((smem_u32(smem_raw) + C128_OFF_B) & 1023u) == 0;
 
     if (w == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
@@ -227,7 +302,7 @@ __global__ void __launch_bounds__(C128_THREADS, 1) chain128_tc_kernel(ChainFacto
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        for (int q = 0; q < 2; ++q)
+        for (int q = 0; q < 2 + C128_NCHUNK + C128_NBBUF; ++q)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbars[q])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         *abort = 0;
@@ -238,7 +313,33 @@ __global__ void __launch_bounds__(C128_THREADS, 1) chain128_tc_kernel(ChainFacto
     tc_fence_after();
     const uint32_t tm = *tslot;
     const uint32_t base_addr = smem_u32(smem_raw);
+    const uint32_t mbA = smem_u32(&mbars[2]), mbB = smem_u32(&mbars[2 + C128_NCHUNK]);
     C64Bar bar[2] = {{smem_u32(&mbars[0]), 0u, false}, {smem_u32(&mbars[1]), 0u, false}};
+    uint32_t a_phase = 0, a_pend = 0, b_phase = 0, b_pend = 0;  // thread 0's view of the copy mbarriers
+
+    // thread 0: A_i column chunk j (16 columns, contiguous) into its buffer
+    auto issue_a = [&](const Tin *Ag, int j) {
+        const int cols = min(16, n - 16 * j);
+        if (cols <= 0) return;
+        const uint32_t bytes = (uint32_t)(cols * n) * (uint32_t)sizeof(Tin);
+        const uint32_t mb = mbA + 8u * (uint32_t)j;
+        mbar_expect_tx(mb, bytes);
+        bulk_g2s(base_addr + (uint32_t)c128_achunk(j), Ag + (long long)16 * j * n, bytes, mb);
+        a_pend |= 1u << j;
+    };
+    // thread 64: B_i row chunk c (rows 16 c .. +15 of the block's 128 columns)
+    // into buffer c % 3 with one tensor copy; thread 0 marks it outstanding
+    auto issue_b = [&](long long blk, int c) {
+        if (16 * c >= n) return;
+        const int b = c % C128_NBBUF;
+        const uint32_t mb = mbB + 8u * (uint32_t)b;
+        if (tid == 64) {
+            fence_async_smem();
+            mbar_expect_tx(mb, (uint32_t)(16 * 128 * sizeof(Tin)));  // the whole box, zero-filled parts included
+            tma_load_2d(base_addr + (uint32_t)(C128_OFF_B + b * C128_BCH), &tmB, 16 * c, (int)(blk * n), mb);
+        }
+        if (tid == 0) b_pend |= 1u << b;
+    };
 
     // partitions p = blockIdx.x, + gridDim.x, ... (the grid is at most one CTA per SM)
     for (long long p = blockIdx.x; p < g.Q && !*abort; p += gridDim.x) {
@@ -253,35 +354,70 @@ __global__ void __launch_bounds__(C128_THREADS, 1) chain128_tc_kernel(ChainFacto
     bool sll = false;
     for (long long i = first; i <= last; ++i) {
         const long long t = i - first;
+        const Tin *Ag = g.A_in + i * nn;
+        const Tin *Bg = g.B_in + i * nn;
         if (tid == 32 && pf && i < last) {  // the next step's blocks into L2
             bulk_prefetch_l2(g.A_in + (i + 1) * nn, blk_bytes);
             bulk_prefetch_l2(g.B_in + (i + 1) * nn, blk_bytes);
         }
+        // A_i's first chunk has a buffer of its own; at a chain's first step
+        // (no phase 1) every chunk's buffer is free
+        if (tid == 0 && bulk) {
+            fence_async_smem();
+            issue_a(Ag, 0);
+            if (t == 0)
+                for (int j = 1; j < C128_NCHUNK; ++j) issue_a(Ag, j);
+        }
         // ---- phase 1: D1 = W^T W, D2 = Y^T W, S_LL += Y^T Y on the carried rows
         if (t > 0) {
-            if (!c128_phase1(tm, rawW, rawY, smem_raw + C128_OFF_S1, base_addr + C128_OFF_S1, bar, abort, sll, tid))
+            auto rows_read = [&]() {  // thread 0: the carried-Y region takes A chunks 1-4
+                if (bulk) {
+                    fence_async_smem();
+                    for (int j = 1; j <= 4; ++j) issue_a(Ag, j);
+                }
+            };
+            if (!c128_phase1(tm, rawW, rawY, smem_raw + C128_OFF_S1, base_addr + C128_OFF_S1, bar, abort, sll, tid,
+                             rows_read))
                 break;
             sll = true;
+            if (tid == 0 && bulk)  // the drained phase-1 stages take A chunks 5-7
+                for (int j = 5; j < C128_NCHUNK; ++j) issue_a(Ag, j);
         }
         // ---- Ahat_i = A_i - D1 into sS (identity outside n x n); sS overlays the carried W, read by now
-        {
-            const Tin *Ag = g.A_in + i * nn;
+        if (bulk) {
+            // chunk by chunk as the copies land: this thread's row L, 8 columns of the chunk
+            const int h = w >> 2;
+#pragma unroll 1
+            for (int j = 0; j < C128_NCHUNK; ++j) {
+                if (tid == 0) c128_waitbit(mbA + 8u * (uint32_t)j, j, a_phase, a_pend, abort);
+                __syncthreads();
+                if (*abort) break;
+                const int c0 = 16 * j + 8 * h;
+                float d[8];
+                if (t > 0) {
+                    c128_ld8(tm + lane_base + C128_T_D1 + (uint32_t)c0, d);
+                } else {
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) d[u] = 0.f;
+                }
+                const Tin *ach = reinterpret_cast<const Tin *>(smem_raw + c128_achunk(j));
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int c = c0 + u;
+                    sS[L + c * LD] = (L < n && c < n) ? (float)ach[(c - 16 * j) * n + L] - d[u] : (L == c ? 1.f : 0.f);
+                }
+            }
+            if (*abort) break;
+        } else {
 #pragma unroll 1
             for (int hf = 0; hf < 2; ++hf) {
                 const int c0 = cb + 32 * hf;
-                // every load is issued (clamped to a valid address) before any is
-                // used, so a thread has its 32 loads in flight at once
+                // every load is issued (clamped to a valid address) before any is used
                 Tin ga[32];
 #pragma unroll
                 for (int q = 0; q < 32; ++q) {
                     const int c = c0 + q;
                     ga[q] = __ldcg(Ag + ((L < n && c < n) ? L + (long long)c * n : 0));
-                }
-                float a[32];
-#pragma unroll
-                for (int q = 0; q < 32; ++q) {
-                    const int c = c0 + q;
-                    a[q] = (L < n && c < n) ? (float)ga[q] : (L == c ? 1.f : 0.f);
                 }
                 float d[32];
                 if (t > 0) {
@@ -291,75 +427,38 @@ __global__ void __launch_bounds__(C128_THREADS, 1) chain128_tc_kernel(ChainFacto
                     for (int q = 0; q < 32; ++q) d[q] = 0.f;
                 }
 #pragma unroll
-                for (int q = 0; q < 32; ++q) sS[L + (c0 + q) * LD] = (L < n && c0 + q < n) ? a[q] - d[q] : a[q];
+                for (int q = 0; q < 32; ++q) {
+                    const int c = c0 + q;
+                    sS[L + c * LD] = (L < n && c < n) ? (float)ga[q] - d[q] : (L == c ? 1.f : 0.f);
+                }
             }
         }
         __syncthreads();
+        // B_i's first chunks land during the Cholesky (the A chunk buffers are read)
+        if (tmab)
+            for (int c = 0; c < C128_NBBUF; ++c) issue_b(i, c);
         // ---- U^T U = Ahat, V = U^-1 (CUDA cores; ends with a CTA barrier)
         const int bad = chol_inv_blocked<float, 128, C128_THREADS, true, true>(sS, sV, dinv, sflag, tid, prow);
         if (bad && tid == 0) record_bad_pivot(g.st, g.level, i);
         // ---- phase 2: D1 = Z^T V = Y_i^T, DW = B^T V = W_i^T; V_i to HBM on the way
         {
-            // this thread's B_i values of every chunk: column rm, rows 16 c + 8 rq .. +7,
-            // all loads issued before any is used (clamped addresses; 16-byte
-            // loads through L1 when n = 128, which keep each sector's second
-            // half for the next load)
-            float bv[C128_NCHUNK][8];
-            const Tin *Bg = g.B_in + i * nn;
-            if (n == 128) {
-                using V2 = typename Vec<Tin>::type;
-                constexpr int W2 = Vec<Tin>::W;
-                V2 gb[C128_NCHUNK][8 / W2];
-#pragma unroll
-                for (int c = 0; c < C128_NCHUNK; ++c)
-#pragma unroll
-                    for (int u = 0; u < 8 / W2; ++u)
-                        gb[c][u] = __ldg(reinterpret_cast<const V2 *>(Bg + 16 * c + 8 * rq + W2 * u + rm * 128));
-#pragma unroll
-                for (int c = 0; c < C128_NCHUNK; ++c)
-#pragma unroll
-                    for (int u = 0; u < 8 / W2; ++u) {
-                        if constexpr (W2 == 2) {
-                            bv[c][2 * u] = (float)gb[c][u].x;
-                            bv[c][2 * u + 1] = (float)gb[c][u].y;
-                        } else {
-                            bv[c][4 * u] = gb[c][u].x;
-                            bv[c][4 * u + 1] = gb[c][u].y;
-                            bv[c][4 * u + 2] = gb[c][u].z;
-                            bv[c][4 * u + 3] = gb[c][u].w;
-                        }
-                    }
-            } else {
-                Tin gb[C128_NCHUNK][8];
-#pragma unroll
-                for (int c = 0; c < C128_NCHUNK; ++c)
-#pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        const int k = 16 * c + 8 * rq + u;
-                        gb[c][u] = __ldg(Bg + ((rm < n && k < n) ? k + (long long)rm * n : 0));
-                    }
-#pragma unroll
-                for (int c = 0; c < C128_NCHUNK; ++c)
-#pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        const int k = 16 * c + 8 * rq + u;
-                        bv[c][u] = (rm < n && k < n) ? (float)gb[c][u] : 0.f;
-                    }
-            }
             const Tin *Bs = g.B_in + sL * nn;  // Z_first = B_sL^T
             float *Vg = g.A_f + i * nn;
-#pragma unroll
+#pragma unroll 1
             for (int c = 0; c < C128_NCHUNK; ++c) {
-                const int s = c & 1;
-                if (tid == 0) c64_wait1(bar[s], abort);
+                const int s = c & 1, bb = c % C128_NBBUF;
+                if (tid == 0) {
+                    c64_wait1(bar[s], abort);
+                    if (tmab) c128_waitbit(mbB + 8u * (uint32_t)bb, bb, b_phase, b_pend, abort);
+                }
                 tc_fence_before();
                 __syncthreads();
                 if (*abort) break;
                 unsigned char *st = smem_raw + C128_OFF_X + s * C128_STAGE2;
                 // V: op(V) row m = column m of V (zero below the diagonal tiles)
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int q = rq + 2 * h, k = 16 * c + 4 * q;
+                for (int hq = 0; hq < 2; ++hq) {
+                    const int q = rq + 2 * hq, k = 16 * c + 4 * q;
                     float4 v = *reinterpret_cast<const float4 *>(sV + k + rm * LD);
                     if ((k >> 4) > (rm >> 4)) v = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (n == 128) {
@@ -372,11 +471,47 @@ __global__ void __launch_bounds__(C128_THREADS, 1) chain128_tc_kernel(ChainFacto
                     }
                     c128_put4(st + 4 * C128_PART, st + 5 * C128_PART, c128_off(rm, 4 * q), v.x, v.y, v.z, v.w);
                 }
-                // B: op(B) row m = column m of B_i
+                // B: op(B) row m = column m of B_i, rows 16 c + 8 rq .. +7
+                {
+                    float bv[8];
+                    if (tmab) {
+                        // column rm of the box, values 8 rq .. 8 rq + 7 (zero-filled outside the block)
+                        const unsigned char *buf = smem_raw + C128_OFF_B + bb * C128_BCH;
 #pragma unroll
-                for (int h = 0; h < 2; ++h)
-                    c128_put4(st + 2 * C128_PART, st + 3 * C128_PART, c128_off(rm, 8 * rq + 4 * h), bv[c][4 * h],
-                              bv[c][4 * h + 1], bv[c][4 * h + 2], bv[c][4 * h + 3]);
+                        for (int u = 0; u < 8; u += 16 / (int)sizeof(Tin)) {
+                            const uint32_t off = (uint32_t)((rm * 16 + 8 * rq + u) * (int)sizeof(Tin));
+                            const uint4 raw = *reinterpret_cast<const uint4 *>(buf + c128_swz(off));
+                            if constexpr (sizeof(Tin) == 8) {
+                                bv[u] = (float)__hiloint2double((int)raw.y, (int)raw.x);
+                                bv[u + 1] = (float)__hiloint2double((int)raw.w, (int)raw.z);
+                            } else {
+                                bv[u] = __uint_as_float(raw.x);
+                                bv[u + 1] = __uint_as_float(raw.y);
+                                bv[u + 2] = __uint_as_float(raw.z);
+                                bv[u + 3] = __uint_as_float(raw.w);
+                            }
+                        }
+#pragma unroll
+                        for (int u = 0; u < 8; ++u)
+                            if (rm >= n || 16 * c + 8 * rq + u >= n) bv[u] = 0.f;
+                    } else {
+                        Tin gb[8];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const int k = 16 * c + 8 * rq + u;
+                            gb[u] = __ldg(Bg + ((rm < n && k < n) ? k + (long long)rm * n : 0));
+                        }
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const int k = 16 * c + 8 * rq + u;
+                            bv[u] = (rm < n && k < n) ? (float)gb[u] : 0.f;
+                        }
+                    }
+#pragma unroll
+                    for (int hq = 0; hq < 2; ++hq)
+                        c128_put4(st + 2 * C128_PART, st + 3 * C128_PART, c128_off(rm, 8 * rq + 4 * hq), bv[4 * hq],
+                                  bv[4 * hq + 1], bv[4 * hq + 2], bv[4 * hq + 3]);
+                }
                 // Z: op(Z) row m = column m of Z_i = -(row m of D2); Z_first = B_sL^T
                 {
                     const int kz = 8 * (w >> 2);
@@ -407,6 +542,8 @@ __global__ void __launch_bounds__(C128_THREADS, 1) chain128_tc_kernel(ChainFacto
                     tc_commit(bar[s].addr);
                     bar[s].pending = true;
                 }
+                // the B buffer just split takes the chunk three ahead
+                if (tmab && c + C128_NBBUF < C128_NCHUNK) issue_b(i, c + C128_NBBUF);
             }
         }
         if (tid == 0) c128_drain(bar, abort);
@@ -434,7 +571,8 @@ __global__ void __launch_bounds__(C128_THREADS, 1) chain128_tc_kernel(ChainFacto
 
     // ---- chain end: S_RR = W^T W (D1), S_LR = Y^T W (D2), S_LL += Y^T Y
     if (!*abort && first <= last) {
-        if (c128_phase1(tm, rawW, rawY, smem_raw + C128_OFF_S1, base_addr + C128_OFF_S1, bar, abort, sll, tid)) {
+        if (c128_phase1(tm, rawW, rawY, smem_raw + C128_OFF_S1, base_addr + C128_OFF_S1, bar, abort, sll, tid,
+                        []() {})) {
             float *Cp = g.C + p * 3 * nn;
 #pragma unroll 1
             for (int hf = 0; hf < 2; ++hf) {
@@ -458,11 +596,13 @@ __global__ void __launch_bounds__(C128_THREADS, 1) chain128_tc_kernel(ChainFacto
     }  // partitions
     __syncthreads();
     if (*abort && tid == 0) {
-        // a wait gave up: wait (bounded) for this CTA's MMAs still in flight
-        // before its shared memory and TMEM are released
+        // a wait gave up: wait (bounded) for this CTA's MMAs and copies still
+        // in flight before its shared memory and TMEM are released
         int ignored = 0;
         c64_wait1(bar[0], &ignored);
         c64_wait1(bar[1], &ignored);
+        for (int j = 0; j < C128_NCHUNK; ++j) c128_waitbit(mbA + 8u * (uint32_t)j, j, a_phase, a_pend, &ignored);
+        for (int b = 0; b < C128_NBBUF; ++b) c128_waitbit(mbB + 8u * (uint32_t)b, b, b_phase, b_pend, &ignored);
         if (g.st) atomicExch(&g.st->tc_timeout, 1);
     }
     tc_fence_before();

@@ -36,6 +36,7 @@
 // Each thread owns the RA x RB elements (ti + TI*a, tj + TJ*b) of a tile.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 

@@ -1,6 +1,8 @@
 // Launcher definitions, included by the per-dtype kernel translation units.
 #pragma once
 
+#include <cstring>
+
 #include "bss_launch.h"
 
 namespace bss {
@@ -67,10 +69,44 @@ static bool use_chain128(const ChainFactorArgs<Tin, float> &a)
     return !a.seq && a.n <= 128 && !(a.variant & FACTOR_WIDE_L2);
 }
 
+// tensor map of a level's B blocks for chain128_tc_kernel: a 2D FP64 tensor
+// of n rows x (N - 1) n columns (column stride n * 8 bytes), boxes of 16 rows
+// x 128 columns, 128-byte swizzle, zero fill outside.  False (the kernel then
+// reads B with plain loads) when the layout does not qualify or the driver
+// entry point is missing.
+template <class Tin>
+bool chain128_tmap_b(const ChainFactorArgs<Tin, float> &a, CUtensorMap *map)
+{
+    std::memset(map, 0, sizeof(*map));
+    if (sizeof(Tin) != 8 || a.n % 2 != 0 || a.N < 2 || ((uintptr_t)a.B_in % 16u) != 0) return false;
+    using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static Encode encode = []() -> Encode {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return reinterpret_cast<Encode>(fn);
+    }();
+    if (!encode) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)a.n, (cuuint64_t)(a.N - 1) * (cuuint64_t)a.n};
+    const cuuint64_t strides[1] = {(cuuint64_t)a.n * sizeof(Tin)};
+    const cuuint32_t box[2] = {16u, 128u};
+    const cuuint32_t estr[2] = {1u, 1u};
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<Tin *>(a.B_in), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <class Tin>
 static cudaError_t chain128_tc(const ChainFactorArgs<Tin, float> &a, cudaStream_t s)
 {
     const size_t smem = chain128_tc_smem();
+    CUtensorMap tmB;
+    const int tma_b = chain128_tmap_b<Tin>(a, &tmB) ? 1 : 0;
     auto kern = chain128_tc_kernel<Tin>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -79,7 +115,7 @@ static cudaError_t chain128_tc(const ChainFactorArgs<Tin, float> &a, cudaStream_
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const unsigned grid = (unsigned)(a.Q < sms ? a.Q : sms);  // one CTA per SM walks several partitions
-    kern<<<grid, C128_THREADS, smem, s>>>(a);
+    kern<<<grid, C128_THREADS, smem, s>>>(a, tmB, tma_b);
     count_launch();
     return cudaGetLastError();
 }
