@@ -586,18 +586,18 @@ __device__ __forceinline__ int warp_chol_row(float *sS, float *dinv, float *row,
 }
 
 // trailing update of panel o in FP32: S(a, b) -= sum_p U(o+p, a) U(o+p, b)
-// over the whole trailing block (the Cholesky reads only its upper
-// triangle): lanes take rows a (a + 32, ... up to the tile), warps take columns b; a thread
-// keeps its U columns in registers and reads each U(., b) as a broadcast, all
-// in 128-bit steps (column reads conflict-free for LD = NB + 4)
-template <int LD, int NB, int PB, int THREADS>
-__device__ __forceinline__ void trailing_update_f32(float *sS, int o, int tid)
+// for the trailing columns b >= bfirst (relative to the trailing block),
+// over nw warps (this one is warp wi of them): lanes take rows a (a + 32,
+// ... up to the tile), warps take columns b; a thread keeps its U columns in
+// registers and reads each U(., b) as a broadcast, all in 128-bit steps
+// (column reads conflict-free for LD = NB + 4).  The Cholesky reads only the
+// upper triangle, so row groups wholly below the diagonal are skipped.
+template <int LD, int NB, int PB>
+__device__ __forceinline__ void trailing_update_f32(float *sS, int o, int bfirst, int wi, int nw, int lane)
 {
     static_assert(PB == 16, "four float4 per column segment");
-    constexpr int NW = THREADS / 32;
     constexpr int H = (NB - PB + 31) / 32;  // row groups of 32 per lane
     const int m = NB - o - PB, c0 = o + PB;
-    const int warp = tid >> 5, lane = tid & 31;
     float4 ua[H][4];
 #pragma unroll
     for (int h = 0; h < H; ++h) {
@@ -607,20 +607,40 @@ __device__ __forceinline__ void trailing_update_f32(float *sS, int o, int tid)
             for (int q = 0; q < 4; ++q) ua[h][q] = *reinterpret_cast<const float4 *>(sS + o + 4 * q + (c0 + a) * LD);
         }
     }
-    for (int b = warp; b < m; b += NW) {
+    for (int b = bfirst + wi; b < m; b += nw) {
         float4 ub[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) ub[q] = *reinterpret_cast<const float4 *>(sS + o + 4 * q + (c0 + b) * LD);
 #pragma unroll
         for (int h = 0; h < H; ++h) {
             const int a = lane + 32 * h;
-            if (a < m) {
+            if (a < m && 32 * h <= b) {
                 float acc = 0.f;
 #pragma unroll
                 for (int q = 0; q < 4; ++q) fma_vec(acc, ua[h][q], ub[q]);
                 sS[(c0 + a) + (c0 + b) * LD] -= acc;
             }
         }
+    }
+}
+
+// the next diagonal tile of panel o (rows and columns o + PB .. o + 2 PB - 1)
+// updated by one warp: lane l takes column b = l % 16 and rows 8 (l / 16) .. +7
+template <int LD, int PB>
+__device__ __forceinline__ void tile_update_f32(float *sS, int o, int lane)
+{
+    static_assert(PB == 16, "four float4 per column segment");
+    const int c0 = o + PB, b = lane & 15, a0 = (lane >> 4) * 8;
+    float4 ub[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ub[q] = *reinterpret_cast<const float4 *>(sS + o + 4 * q + (c0 + b) * LD);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int a = a0 + r;
+        float acc = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) fma_vec(acc, *reinterpret_cast<const float4 *>(sS + o + 4 * q + (c0 + a) * LD), ub[q]);
+        sS[(c0 + a) + (c0 + b) * LD] -= acc;
     }
 }
 
@@ -679,6 +699,13 @@ __device__ __forceinline__ void inv_column_par(float *sS, float *sV, int J, int 
 // column K-1; then warp 1 inverts the diagonal tile while the rest solve the
 // row panel; then the trailing update.  V's last block column follows the
 // loop (FP32); FP64 forms V's off-diagonal tiles in stages after it.
+// The FAST form of tiles of 128 and more looks one panel ahead: once panel
+// K's row panel is solved, warp 0 updates only the next diagonal tile and
+// factors it at once, while the other warps update the rest of the trailing
+// matrix and then form V's block column K (its diagonal tile was inverted
+// with the row panel).  Measured on GB300 in the chain kernels: the 128 tile
+// 71K -> 62K cycles per step; the 64 tile (four panels) gained nothing, and
+// keeps the panel-by-panel order.
 // INL: the panel helpers are inlined into the caller (no call saves and
 // restores of the caller's registers on the critical warp); the default
 // calls them out of line, which keeps register-heavy callers from spilling.
@@ -695,6 +722,38 @@ __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sfla
     constexpr int KP = NB / PB;
     const int warp = tid >> 5, lane = tid & 31;
     if (tid == 0) *sflag = 0;
+    if constexpr (FAST && NB >= 128) {
+        if (warp == 0) {
+            const int bad = warp_chol_row<LD, PB>(sS, dinv, row, 0, lane);
+            if (bad && lane == 0) *sflag = 1;
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int K = 0; K < KP; ++K) {
+            const int o = PB * K;
+            // V_KK (warp 1) and the row panel U(K, K+1:) (the others)
+            if (warp == 1)
+                warp_inv_i<T, LD, PB>(sS, dinv, sV, o, lane);
+            else if (K + 1 < KP)
+                panel_trsm_i<T, LD, NB, PB>(sS, dinv, o, warp == 0 ? lane : tid - 32, THREADS - 32);
+            __syncthreads();
+            if (K + 1 < KP) {
+                if (warp == 0) {  // the next diagonal tile, updated and factored by one warp
+                    tile_update_f32<LD, PB>(sS, o, lane);
+                    __syncwarp();
+                    const int bad = warp_chol_row<LD, PB>(sS, dinv, row, o + PB, lane);
+                    if (bad && lane == 0) *sflag = 1;
+                } else {  // the rest of the trailing matrix, then V's block column K
+                    trailing_update_f32<LD, NB, PB>(sS, o, PB, warp - 1, THREADS / 32 - 1, lane);
+                    if (K >= 1) inv_column_par<LD, PB>(sS, sV, K, tid - 32, THREADS - 32, 1);
+                }
+            } else if (K >= 1) {
+                inv_column_par<LD, PB>(sS, sV, K, tid, THREADS, 0);  // the last block column, all threads
+            }
+            __syncthreads();
+        }
+        return *sflag;
+    } else {
 #pragma unroll 1
     for (int K = 0; K < KP; ++K) {
         const int o = PB * K;
@@ -732,7 +791,7 @@ __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sfla
             }
             __syncthreads();
             if constexpr (FAST)
-                trailing_update_f32<LD, NB, PB, THREADS>(sS, o, tid);
+                trailing_update_f32<LD, NB, PB>(sS, o, 0, warp, THREADS / 32, lane);
             else if constexpr (INL)
                 trailing_update_i<T, LD, NB, PB>(sS, o, tid, THREADS);
             else
@@ -752,6 +811,7 @@ __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sfla
         __syncthreads();
     }
     return *sflag;
+    }
 }
 
 // ---------------------------------------------------------------------------
