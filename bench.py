@@ -50,7 +50,9 @@ def parse():
                          "chain_n64 (N=4096, n=64, mixed), wide_n128 (N=2048, n=128, mixed), "
                          "headline_eager (N=16384, n=64, mixed, no CUDA graphs: every kernel a launch), "
                          "csr_n64 (CSR assembly of N=4096, n=64), chain_n64_k16 (N=4096, n=64, k=16, mixed), "
-                         "batch_small (64 uneven systems, mixed), batch_2048 (the 2048-system batch, mixed)")
+                         "batch_small (64 uneven systems, mixed), batch_2048 (the 2048-system batch, mixed), "
+                         "wide_n128_k4 (N=4096, n=128, k=4, mixed, no CUDA graphs), "
+                         "wide_n128_k4_16k (N=16384, n=128, k=4, mixed, no CUDA graphs)")
     return ap.parse_args()
 
 
@@ -1176,16 +1178,16 @@ def run_case(name, reps=3):
     import blockstructuredsolvers_gb300 as bss
     dev = torch.device("cuda", 0)
     g = torch.Generator(device=dev).manual_seed(5)
-    if name in ("chain_n64", "chain_n64_k16", "wide_n128", "headline_eager"):
+    if name in ("chain_n64", "chain_n64_k16", "wide_n128", "headline_eager", "wide_n128_k4", "wide_n128_k4_16k"):
         N, n = {"chain_n64": (4096, 64), "chain_n64_k16": (4096, 64), "wide_n128": (2048, 128),
-                "headline_eager": (N_BLK, N_SZ)}[name]
-        k = 16 if name == "chain_n64_k16" else 1
+                "headline_eager": (N_BLK, N_SZ), "wide_n128_k4": (4096, 128), "wide_n128_k4_16k": (16384, 128)}[name]
+        k = {"chain_n64_k16": 16, "wide_n128_k4": 4, "wide_n128_k4_16k": 4}.get(name, 1)
+        eager = name in ("headline_eager", "wide_n128_k4", "wide_n128_k4_16k")
         G = torch.randn((N, n, n), dtype=torch.float64, device=dev, generator=g)
         A = (G @ G.transpose(1, 2) + n * torch.eye(n, dtype=torch.float64, device=dev)).permute(1, 2, 0)
         B = torch.randn((N - 1, n, n), dtype=torch.float64, device=dev, generator=g).permute(1, 2, 0)
         d = torch.rand((N, n, k), dtype=torch.float64, device=dev, generator=g).permute(1, 2, 0)
-        data = bss.initialize_batched(N, n, torch.float64, k=k, precision="mixed",
-                                      use_graphs=name != "headline_eager")
+        data = bss.initialize_batched(N, n, torch.float64, k=k, precision="mixed", use_graphs=not eager)
         data.A_tensor[:, :, :N].copy_(A)
         data.B_tensor[:, :, :N - 1].copy_(B)
         for _ in range(reps):
