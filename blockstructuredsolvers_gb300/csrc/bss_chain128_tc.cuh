@@ -46,8 +46,8 @@
 // conflicts.  The chunk after the one being multiplied is split while the
 // tensor core works on the current one.
 //
-// Block loads are bulk copies (cp.async.bulk) completing on mbarriers, and
-// both blocks are hinted into L2 (cp.async.bulk.prefetch.L2) a step ahead:
+// Block loads are bulk copies (cp.async.bulk) completing on mbarriers (L2
+// prefetch hints a step ahead measured no gain in time or DRAM bytes):
 // A_i in column chunks of 16 (contiguous in the column-major block), chunk 0
 // issued at the step's start into a buffer of its own, the others as soon
 // as phase 1 has released their buffers; B_i in row chunks of 16 (the K
@@ -287,9 +287,7 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
     const int rm = tid & 127, rq = tid >> 7;  // converter mapping: operand row, K group
     const int n = g.n;
     const long long nn = (long long)n * n;
-    const uint32_t blk_bytes = (uint32_t)(nn * (long long)sizeof(Tin));
     const bool aligned = ((uintptr_t)g.A_in % 16u) == 0 && ((uintptr_t)g.B_in % 16u) == 0;
-    const bool pf = (blk_bytes % 16u) == 0 && aligned;
     // bulk copies of column chunks (A) and the tensor copies of row chunks (B)
     // start on 16 bytes; the latter also need the 1024-byte-aligned buffers
     const bool bulk = aligned && (sizeof(Tin) == 8 ? n % 2 == 0 : n % 4 == 0);
@@ -346,20 +344,11 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
     const long long sL = (p * (g.N - 1)) / g.Q;
     const long long sR = ((p + 1) * (g.N - 1)) / g.Q;
     const long long first = sL + 1, last = sR - 1;
-    if (tid == 0 && pf && first <= last) {
-        bulk_prefetch_l2(g.A_in + first * nn, blk_bytes);
-        bulk_prefetch_l2(g.B_in + first * nn, blk_bytes);
-        bulk_prefetch_l2(g.B_in + sL * nn, blk_bytes);
-    }
     bool sll = false;
     for (long long i = first; i <= last; ++i) {
         const long long t = i - first;
         const Tin *Ag = g.A_in + i * nn;
         const Tin *Bg = g.B_in + i * nn;
-        if (tid == 32 && pf && i < last) {  // the next step's blocks into L2
-            bulk_prefetch_l2(g.A_in + (i + 1) * nn, blk_bytes);
-            bulk_prefetch_l2(g.B_in + (i + 1) * nn, blk_bytes);
-        }
         // A_i's first chunk has a buffer of its own; at a chain's first step
         // (no phase 1) every chunk's buffer is free
         if (tid == 0 && bulk) {
@@ -440,10 +429,9 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
         // ---- U^T U = Ahat, V = U^-1 (CUDA cores; ends with a CTA barrier)
         const int bad = chol_inv_blocked<float, 128, C128_THREADS, true, true>(sS, sV, dinv, sflag, tid, prow);
         if (bad && tid == 0) record_bad_pivot(g.st, g.level, i);
-        // ---- phase 2: D1 = Z^T V = Y_i^T, DW = B^T V = W_i^T; V_i to HBM on the way
+        // ---- phase 2: D1 = Z^T V = Y_i^T, DW = B^T V = W_i^T
         {
             const Tin *Bs = g.B_in + sL * nn;  // Z_first = B_sL^T
-            float *Vg = g.A_f + i * nn;
 #pragma unroll 1
             for (int c = 0; c < C128_NCHUNK; ++c) {
                 const int s = c & 1, bb = c % C128_NBBUF;
@@ -461,14 +449,6 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
                     const int q = rq + 2 * hq, k = 16 * c + 4 * q;
                     float4 v = *reinterpret_cast<const float4 *>(sV + k + rm * LD);
                     if ((k >> 4) > (rm >> 4)) v = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (n == 128) {
-                        *reinterpret_cast<float4 *>(Vg + k + rm * 128) = v;
-                    } else if (rm < n) {
-                        const float vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                        for (int u = 0; u < 4; ++u)
-                            if (k + u < n) Vg[k + u + (long long)rm * n] = vv[u];
-                    }
                     c128_put4(st + 4 * C128_PART, st + 5 * C128_PART, c128_off(rm, 4 * q), v.x, v.y, v.z, v.w);
                 }
                 // B: op(B) row m = column m of B_i, rows 16 c + 8 rq .. +7
@@ -550,6 +530,24 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
         __syncthreads();
         if (*abort) break;
         tc_fence_after();
+        // ---- V_i to HBM in whole lines (column m of V is column m of sV; zero below the diagonal tiles)
+        {
+            float *Vg = g.A_f + i * nn;
+            if (n == 128) {
+                for (int e = tid; e < 128 * 32; e += C128_THREADS) {
+                    const int m = e >> 5, k4 = (e & 31) * 4;
+                    float4 v = *reinterpret_cast<const float4 *>(sV + k4 + m * LD);
+                    if ((k4 >> 4) > (m >> 4)) v = make_float4(0.f, 0.f, 0.f, 0.f);
+                    *reinterpret_cast<float4 *>(Vg + m * 128 + k4) = v;
+                }
+            } else {
+                for (int e = tid; e < n * n; e += C128_THREADS) {
+                    const int m = e / n, k = e - m * n;
+                    Vg[e] = ((k >> 4) > (m >> 4)) ? 0.f : sV[k + m * LD];
+                }
+            }
+        }
+        __syncthreads();  // sV is read: the carried Y rows take its place
         // ---- Y_i, W_i: TMEM rows -> carried rows (next step's operands) -> HBM
 #pragma unroll 1
         for (int hf = 0; hf < 2; ++hf) {

@@ -71,7 +71,9 @@ static bool use_chain128(const ChainFactorArgs<Tin, float> &a)
 
 // tensor map of a level's B blocks for chain128_tc_kernel: a 2D FP64 tensor
 // of n rows x (N - 1) n columns (column stride n * 8 bytes), boxes of 16 rows
-// x 128 columns, 128-byte swizzle, zero fill outside.  False (the kernel then
+// x 128 columns, 128-byte swizzle, zero fill outside; L2 fills of 128 bytes
+// (a box row is 128 bytes: a wider fill would fetch rows the next chunk
+// reads only later).  False (the kernel then
 // reads B with plain loads) when the layout does not qualify or the driver
 // entry point is missing.
 template <class Tin>
@@ -97,7 +99,7 @@ bool chain128_tmap_b(const ChainFactorArgs<Tin, float> &a, CUtensorMap *map)
     const cuuint32_t box[2] = {16u, 128u};
     const cuuint32_t estr[2] = {1u, 1u};
     return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<Tin *>(a.B_in), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 

@@ -20,7 +20,8 @@
 // The forward products (M^T v, one result per column of the slot) give each
 // column 8 lanes that read its rows in interleaved vector chunks and sum by
 // shuffles; the backward product (M x, a result per row) gives each thread
-// whole rows, reading M across lanes without conflicts.
+// four rows and four right-hand sides over a share of the columns, the
+// shares summed through shared memory once per block product.
 //
 // Thread 0 alone waits on the mbarriers (a spin on mbarrier.test_wait,
 // bounded by ~1 s of SM clock); the others meet it at a CTA barrier.  An
@@ -31,19 +32,22 @@
 namespace bss {
 
 // the forward product gives each column of a quarter slot (n / 4 columns) 8
-// lanes and needs whole warps (n a multiple of 16); the backward one gives a
-// thread at most 4 result columns per row
+// lanes and needs whole warps (n a multiple of 16); the backward one holds
+// at most 8 right-hand sides per row group
 template <class T>
 __host__ __device__ constexpr bool solve_streamed(int n, int kc)
 {
-    return n % 16 == 0 && n <= 128 && !solve_staged<T>(n, kc) && kc <= 4 * (SOLVE_THREADS / n);
+    return n % 16 == 0 && n <= 128 && !solve_staged<T>(n, kc) && kc <= 8;
 }
 
-// ring (one block) + 6 vectors of n x kc + 4 mbarriers + abort flag
+// partial sums of the backward product: (column parts) x n x kc <= 4096 elements
+constexpr int STREAM_PARTIAL = 4096;
+
+// ring (one block) + 6 vectors of n x kc + the backward partials + 4 mbarriers + abort flag
 template <class T>
 __host__ __device__ constexpr size_t stream_smem_bytes(int n, int kc)
 {
-    return (size_t)n * n * sizeof(T) + (size_t)6 * n * kc * sizeof(T) + 64;
+    return (size_t)n * n * sizeof(T) + (size_t)6 * n * kc * sizeof(T) + (size_t)STREAM_PARTIAL * sizeof(T) + 64;
 }
 
 struct StreamRing {
@@ -117,27 +121,93 @@ __device__ __forceinline__ void slot_tmul8(const T *sM, int qc, const T *v, T *o
     }
 }
 
-// acc[q] += sum_c M(r, c) x(c0 + c, j_q) over the qc columns of a slot:
-// thread (r, jg) owns row r and columns j_q = jg + tpr * q of the result
-template <class T>
-__device__ __forceinline__ void slot_nmul_acc(const T *sM, int qc, const T *x, int c0, int n, int kc, T (&acc)[4])
+// Backward product mapping: thread (rg, jg, part) owns rows 4 rg .. 4 rg + 3
+// and right-hand sides 4 jg .. 4 jg + 3 of M x, summed over the slot columns
+// c = part, part + np, ...: one 128-bit read of M's column segment (lanes on
+// consecutive row groups: conflict-free) and broadcast reads of x feed 16
+// FMAs; the np column parts are summed through shared memory per block.
+struct BwdMap {
+    int rg, jg, part, np;
+    bool active;
+};
+
+__device__ __forceinline__ BwdMap bwd_map(int n, int kc)
 {
-    const int tpr = (int)blockDim.x / n;
-    const int r = threadIdx.x % n, jg = threadIdx.x / n;
-    if (jg >= tpr) return;
-    for (int c = 0; c < qc; c += 4) {
+    const int ngr = n / 4, njg = (kc + 3) / 4;
+    BwdMap m;
+    m.np = SOLVE_THREADS / (ngr * njg);
+    m.rg = threadIdx.x % ngr;
+    const int rest = threadIdx.x / ngr;
+    m.jg = rest % njg;
+    m.part = rest / njg;
+    m.active = m.part < m.np;
+    return m;
+}
+
+// acc[u][q] += sum_c M(4 rg + u, c) x(c0 + c, 4 jg + q) over this thread's
+// columns of a slot (qc columns, leading dimension n)
+template <class T>
+__device__ __forceinline__ void slot_nmul4(const T *sM, int qc, const T *x, int c0, int n, int kc, const BwdMap &bm,
+                                           T (&acc)[4][4])
+{
+    if (!bm.active) return;
+    const int j0 = 4 * bm.jg;
+    for (int c = bm.part; c < qc; c += bm.np) {
+        const T *mc = sM + (size_t)c * n + 4 * bm.rg;
         T m[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) m[u] = sM[r + (size_t)(c + u) * n];
+        if constexpr (sizeof(T) == 4) {
+            const float4 v = *reinterpret_cast<const float4 *>(mc);
+            m[0] = v.x;
+            m[1] = v.y;
+            m[2] = v.z;
+            m[3] = v.w;
+        } else {
+            const double2 v0 = *reinterpret_cast<const double2 *>(mc);
+            const double2 v1 = *reinterpret_cast<const double2 *>(mc + 2);
+            m[0] = v0.x;
+            m[1] = v0.y;
+            m[2] = v1.x;
+            m[3] = v1.y;
+        }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const int j = jg + tpr * q;
-            if (j < kc) {
+            if (j0 + q < kc) {
+                const T xv = x[c0 + c + (j0 + q) * n];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) acc[q] = fma(m[u], x[c0 + c + u + j * n], acc[q]);
+                for (int u = 0; u < 4; ++u) acc[u][q] = fma(m[u], xv, acc[u][q]);
             }
         }
     }
+}
+
+// the column parts' sums: every thread writes its partial block, then each
+// output e of the n x kc result is the sum over the parts (ends with the
+// outputs handed to `out(e, sum)`; barriers before and after)
+template <class T, class F>
+__device__ __forceinline__ void bwd_reduce(T *red, T (&acc)[4][4], int n, int kc, const BwdMap &bm, F out)
+{
+    const int nkc = n * kc;
+    if (bm.active) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int j = 4 * bm.jg + q;
+            if (j < kc) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) red[bm.part * nkc + j * n + 4 * bm.rg + u] = acc[u][q];
+            }
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[u][q] = T(0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nkc; e += blockDim.x) {
+        T s = T(0);
+        for (int q = 0; q < bm.np; ++q) s += red[q * nkc + e];
+        out(e, s);
+    }
+    __syncthreads();
 }
 
 // one pass of a block through the ring: `use(q, slot)` for each quarter,
@@ -260,7 +330,8 @@ __device__ __forceinline__ void chain_bwd_stream_body(const SolveArgs<T> &g, con
     T *sxL = sz + nkc;
     T *sxn = sxL + nkc;
     T *sxt = sxn + nkc;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(sxt + nkc + 2 * nkc);
+    T *red = sxt + 3 * nkc;  // STREAM_PARTIAL elements
+    uint64_t *bars = reinterpret_cast<uint64_t *>(red + STREAM_PARTIAL);
     int *abort = reinterpret_cast<int *>(bars + 4);
     const long long sL = (p * (g.N - 1)) / g.Q;
     const long long sR = ((p + 1) * (g.N - 1)) / g.Q;
@@ -275,44 +346,32 @@ __device__ __forceinline__ void chain_bwd_stream_body(const SolveArgs<T> &g, con
     __syncthreads();
     store_rhs(g.d, sxL, sL, n, g.k, g.j0, kc);
     if (p == g.Q - 1) store_rhs(g.d, sxn, sR, n, g.k, g.j0, kc);
-    const int tpr = (int)blockDim.x / n;
-    const int r = threadIdx.x % n, jg = threadIdx.x / n;
+    const BwdMap bm = bwd_map(n, kc);
+    T acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[u][q] = T(0);
     for (long long i = last; i >= first; --i) {
         if (threadIdx.x == 64 && i > first)
             bulk_prefetch_l2(rhs_ptr<T>(g.d, i - 1, n, g.k, g.j0), (uint32_t)(nkc * sizeof(T)));
         load_rhs(sz, g.d, i, n, g.k, g.j0, kc);
-        T acc[4] = {T(0), T(0), T(0), T(0)};
         // acc = Y_i x_L (ring: Y_i, then W_i)
         if (!ring_pass<T>(rg, ring, qelems, g.Bf + i * (long long)nn, g.Af + i * (long long)nn, abort,
-                          [&](int q, const T *slot) { slot_nmul_acc<T>(slot, qc, sxL, q * qc, n, kc, acc); }))
+                          [&](int q, const T *slot) { slot_nmul4<T>(slot, qc, sxL, q * qc, n, kc, bm, acc); }))
             return ring_abort(rg, g.st);
         // acc += W_i x_{i+1} (ring: W_i, then V_i)
         const T *prevY = i > first ? g.Y + (i - 1) * (long long)nn : (const T *)nullptr;
         if (!ring_pass<T>(rg, ring, qelems, g.Af + i * (long long)nn, prevY, abort,
-                          [&](int q, const T *slot) { slot_nmul_acc<T>(slot, qc, sxn, q * qc, n, kc, acc); }))
+                          [&](int q, const T *slot) { slot_nmul4<T>(slot, qc, sxn, q * qc, n, kc, bm, acc); }))
             return ring_abort(rg, g.st);
-        if (jg < tpr) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int j = jg + tpr * q;
-                if (j < kc) sz[r + j * n] -= acc[q];
-                acc[q] = T(0);
-            }
-        }
-        __syncthreads();
+        bwd_reduce<T>(red, acc, n, kc, bm, [&](int e, T s) { sz[e] -= s; });
         // x_i = V_i z (ring: V_i, then Y_{i-1})
         const T *prevW = i > first ? g.Bf + (i - 1) * (long long)nn : (const T *)nullptr;
         if (!ring_pass<T>(rg, ring, qelems, prevY, prevW, abort,
-                          [&](int q, const T *slot) { slot_nmul_acc<T>(slot, qc, sz, q * qc, n, kc, acc); }))
+                          [&](int q, const T *slot) { slot_nmul4<T>(slot, qc, sz, q * qc, n, kc, bm, acc); }))
             return ring_abort(rg, g.st);
-        if (jg < tpr) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int j = jg + tpr * q;
-                if (j < kc) sxt[r + j * n] = acc[q];
-            }
-        }
-        __syncthreads();
+        bwd_reduce<T>(red, acc, n, kc, bm, [&](int e, T s) { sxt[e] = s; });
         for (int e = threadIdx.x; e < nkc; e += blockDim.x) sxn[e] = sxt[e];
         store_rhs(g.d, sxt, i, n, g.k, g.j0, kc);
         __syncthreads();
