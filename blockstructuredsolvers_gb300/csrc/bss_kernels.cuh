@@ -2511,18 +2511,27 @@ __host__ __device__ constexpr size_t residual_df_smem_cap()
 
 // shared memory of residual_body_df: staged B_i (n (n+1)), x ring (3 nk),
 // u ping-pong (2 nk) and the t / u partials (2 parts nk) as (hi, lo) pairs,
-// plus the FP32 norm partials (25 n)
-template <int THREADS>
+// plus the FP32 norm partials (25 n); with RAW, the raw FP64 A_i and B_i
+// (16-byte aligned) and their mbarrier
+template <int THREADS, bool RAW = false>
 __host__ __device__ constexpr size_t residual_df_smem_bytes(int n, int k)
 {
-    return (size_t)(n * (n + 1) + 5 * n * k + 2 * res_parts<THREADS>(n) * n * k) * 8 + (size_t)25 * n * 4;
+    return ((((size_t)(n * (n + 1) + 5 * n * k + 2 * res_parts<THREADS>(n) * n * k) * 8 + (size_t)25 * n * 4) + 15) /
+            16 * 16) +
+           (RAW ? (size_t)2 * n * n * 8 + 16 : 0);
 }
 
 // Same decomposition as residual_body (thread = (row, column part); B_i
 // staged in shared memory for u_{i+1} = B_i^T x_i; x ring and u ping-pong in
 // shared memory), in double-float: shared arrays hold (hi, lo) float pairs.
-// Shared memory: residual_df_smem_bytes<THREADS>(n, k).
-template <class Tr, int THREADS>
+// Shared memory: residual_df_smem_bytes<THREADS, RAW>(n, k).
+// RAW (even n, 16-byte-aligned A and B): each block's FP64 A_i and B_i come
+// into shared memory by bulk copies (cp.async.bulk on an mbarrier), the next
+// block's issued as soon as this block's first phase has read them, so the
+// copy runs during the second and third phases (and the other CTAs' work);
+// thread 0 alone waits, bounded by ~1 s of SM clock, and an expired wait
+// stops the CTA and records a timeout in the status.
+template <class Tr, int THREADS, bool RAW = false>
 __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, const double *__restrict__ B,
                                                  const double *__restrict__ x, const double *__restrict__ d,
                                                  Tr *__restrict__ r, long long N, int n, int ktot, int j0, int k,
@@ -2548,6 +2557,30 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
     const long long b0 = b0_;
     const long long b1 = b1_ < N ? b1_ : N;
     if (b0 >= N) return;
+    // RAW: A_i, B_i in shared memory (after the arrays above, 16-byte aligned)
+    const size_t raw_off = residual_df_smem_bytes<THREADS, false>(n, k);
+    double *rawA = reinterpret_cast<double *>(smem_raw + raw_off);
+    double *rawB = rawA + nn;
+    uint64_t *rbar = reinterpret_cast<uint64_t *>(rawB + nn);
+    int *rabort = reinterpret_cast<int *>(rbar + 1);
+    const uint32_t raw_bytes = (uint32_t)(nn * 8);
+    uint32_t rphase = 0;
+    auto issue_raw = [&](long long blk) {  // thread 0: A_blk (and B_blk when it exists)
+        const uint32_t mb = smem_u32(rbar);
+        const bool hb = blk + 1 < N;
+        fence_async_smem();
+        mbar_expect_tx(mb, hb ? 2u * raw_bytes : raw_bytes);
+        bulk_g2s(smem_u32(rawA), A + blk * nn, raw_bytes, mb);
+        if (hb) bulk_g2s(smem_u32(rawB), B + blk * nn, raw_bytes, mb);
+    };
+    if constexpr (RAW) {
+        if (tid == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(rbar)) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            *rabort = 0;
+            issue_raw(b0);
+        }
+    }
     if (with_norm < 0) with_norm = st->need_anorm;  // graph mode: decided on the device
     float rmax = 0.0f, xmax = 0.0f, amax = 0.0f;
     auto xs = [&](long long blk) { return sxr + (int)((blk - b0 + 3) % 3) * nk; };  // blk in [b0-1, b1]
@@ -2592,15 +2625,28 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
         const float2 *x1 = xs(i + 1);
         float2 *su = sub + par * nk;         // u_i
         float2 *sun = sub + (par ^ 1) * nk;  // u_{i+1}
-        // phase 1: t partials from global A_i, B_i; B_i into shared memory
-        // (the next block's A and B are hinted into L2 meanwhile)
-        if (i + 1 < b1) {
+        // phase 1: t partials from A_i, B_i; B_i into shared memory (split).
+        // RAW: A_i, B_i from their bulk copies; else from global memory, the
+        // next block's A and B hinted into L2 meanwhile
+        if constexpr (RAW) {
+            if (tid == 0) {
+                const long long t0 = clock64();
+                while (!mbar_test(smem_u32(rbar), rphase))
+                    if (clock64() - t0 > C64_WAIT_CYCLES) {
+                        *rabort = 1;
+                        break;
+                    }
+                rphase ^= 1u;
+            }
+            __syncthreads();
+            if (*rabort) break;
+        } else if (i + 1 < b1) {
             prefetch_l2(A + (i + 1) * nn, (size_t)nn * sizeof(double));
             if (i + 2 < N) prefetch_l2(B + (i + 1) * nn, (size_t)nn * sizeof(double));
         }
         if (active) {
-            const double *Ag = A + i * nn + row;
-            const double *Bg = B + i * nn + row;
+            const double *Ag = (RAW ? rawA : A + i * nn) + row;
+            const double *Bg = (RAW ? rawB : B + i * nn) + row;
             // right-hand sides in compile-time groups (4, then 1); the first
             // group also stages B_i and, when asked, the |A| + |B| row sums
             float *rs = rowred + part * n + row;
@@ -2627,6 +2673,9 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
                                            o + jb * n, n, rs);
         }
         __syncthreads();
+        if constexpr (RAW) {  // A_i and B_i are read: the next block's copies
+            if (tid == 0 && i + 1 < b1) issue_raw(i + 1);
+        }
         // phase 2: u_{i+1} partials from the staged B_i
         if (active && has_b) {
             for (int j = 0; j < k; ++j) {
@@ -2689,6 +2738,17 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
         }
         __syncthreads();
     }
+    if constexpr (RAW) {
+        if (*rabort) {  // a copy wait expired: wait (bounded) for the copy in flight, record, stop
+            if (tid == 0) {
+                const long long t0 = clock64();
+                while (!mbar_test(smem_u32(rbar), rphase) && clock64() - t0 < C64_WAIT_CYCLES) {
+                }
+                atomicExch(&st->tc_timeout, 1);
+            }
+            return;
+        }
+    }
     for (int o = 16; o > 0; o >>= 1) {
         rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
         xmax = fmaxf(xmax, __shfl_xor_sync(0xffffffffu, xmax, o));
@@ -2701,14 +2761,14 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
     }
 }
 
-template <class Tr, int THREADS>
-__global__ void __launch_bounds__(THREADS, THREADS == 256 ? 3 : 1)
+template <class Tr, int THREADS, bool RAW = false>
+__global__ void __launch_bounds__(THREADS, THREADS == 256 ? (RAW ? 2 : 3) : 1)
     residual_df_kernel(const double *__restrict__ A, const double *__restrict__ B, const double *__restrict__ x,
                        const double *__restrict__ d, Tr *__restrict__ r, long long N, int n, int ktot, int j0, int k,
                        long long per_cta, int with_norm, DevStatus *st)
 {
     const long long b0 = (long long)blockIdx.x * per_cta;
-    residual_body_df<Tr, THREADS>(A, B, x, d, r, N, n, ktot, j0, k, b0, b0 + per_cta, with_norm, st);
+    residual_body_df<Tr, THREADS, RAW>(A, B, x, d, r, N, n, ktot, j0, k, b0, b0 + per_cta, with_norm, st);
 }
 
 // many systems: one CTA per (system, block range) item

@@ -324,10 +324,14 @@ template <class Tr, int THREADS>
 cudaError_t launch_residual_df_t(const double *A, const double *B, const double *x, const double *d, Tr *r,
                                  long long N, int n, int k, int with_norm, DevStatus *st, cudaStream_t s)
 {
-    auto kern = residual_df_kernel<Tr, THREADS>;
     int kc = k;  // every column in one pass when the partials fit: A and B are read once
     while (kc > 1 && residual_df_smem_bytes<THREADS>(n, kc) > residual_df_smem_cap<THREADS>()) kc = (kc + 1) / 2;
-    const size_t smem = residual_df_smem_bytes<THREADS>(n, kc);
+    // blocks through bulk copies into shared memory when all columns go in one
+    // pass and two CTAs still fit an SM (256-thread CTAs; even n, aligned A, B)
+    const bool raw = THREADS == 256 && kc == k && n % 2 == 0 && ((uintptr_t)A % 16u) == 0 &&
+                     ((uintptr_t)B % 16u) == 0 && residual_df_smem_bytes<THREADS, true>(n, k) <= (size_t)113 * 1024;
+    auto kern = raw ? residual_df_kernel<Tr, THREADS, true> : residual_df_kernel<Tr, THREADS, false>;
+    const size_t smem = raw ? residual_df_smem_bytes<THREADS, true>(n, kc) : residual_df_smem_bytes<THREADS>(n, kc);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);

@@ -307,4 +307,65 @@ __device__ __forceinline__ void tc_store(const TcCtx &c, float *dst, int n, floa
     __syncthreads();
 }
 
+// ---- bulk copies and the bounded mbarrier waits of the copy-fed kernels ----
+constexpr long long C64_WAIT_CYCLES = 2000000000LL;  // ~1 s of SM clock
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+// one bulk copy global -> shared (16-byte aligned, size a multiple of 16),
+// completing `bytes` of transaction count on the mbarrier
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
+// an mbarrier and the parity of its outstanding phase (thread 0's view)
+struct C64Bar {
+    uint32_t addr;
+    uint32_t phase;
+    bool pending;
+};
+
+__device__ __forceinline__ bool mbar_test(uint32_t mbar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// thread 0 only: wait for the outstanding phase, at most C64_WAIT_CYCLES; on
+// expiry set the abort flag and leave the phase outstanding (drained before
+// exit).  The other threads learn the outcome at the next CTA barrier.
+__device__ __forceinline__ void c64_wait1(C64Bar &b, int *abort)
+{
+    if (!b.pending) return;
+    const long long t0 = clock64();
+    for (;;) {
+        if (mbar_test(b.addr, b.phase)) {
+            b.phase ^= 1u;
+            b.pending = false;
+            return;
+        }
+        if (clock64() - t0 > C64_WAIT_CYCLES) {
+            *abort = 1;
+            return;
+        }
+    }
+}
+
 }  // namespace bss
