@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
                     const int c = c0 + u;
-                    sS[L + c * LD] = (L < n && c < n) ? (float)ach[(c - 16 * j) * n + L] - d[u] : (L == c ? 1.f : 0.f);
+                    sS[L + c * LD] = (L < n && c < n) ? f64_to_f32(ach[(c - 16 * j) * n + L]) - d[u] : (L == c ? 1.f : 0.f);
                 }
             }
             if (*abort) break;
@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
 #pragma unroll
                 for (int q = 0; q < 32; ++q) {
                     const int c = c0 + q;
-                    sS[L + c * LD] = (L < n && c < n) ? (float)ga[q] - d[q] : (L == c ? 1.f : 0.f);
+                    sS[L + c * LD] = (L < n && c < n) ? f64_to_f32(ga[q]) - d[q] : (L == c ? 1.f : 0.f);
                 }
             }
         }
@@ -462,8 +462,8 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
                             const uint32_t off = (uint32_t)((rm * 16 + 8 * rq + u) * (int)sizeof(Tin));
                             const uint4 raw = *reinterpret_cast<const uint4 *>(buf + c128_swz(off));
                             if constexpr (sizeof(Tin) == 8) {
-                                bv[u] = (float)__hiloint2double((int)raw.y, (int)raw.x);
-                                bv[u + 1] = (float)__hiloint2double((int)raw.w, (int)raw.z);
+                                bv[u] = f64_to_f32(__hiloint2double((int)raw.y, (int)raw.x));
+                                bv[u + 1] = f64_to_f32(__hiloint2double((int)raw.w, (int)raw.z));
                             } else {
                                 bv[u] = __uint_as_float(raw.x);
                                 bv[u + 1] = __uint_as_float(raw.y);
@@ -484,7 +484,7 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
 #pragma unroll
                         for (int u = 0; u < 8; ++u) {
                             const int k = 16 * c + 8 * rq + u;
-                            bv[u] = (rm < n && k < n) ? (float)gb[u] : 0.f;
+                            bv[u] = (rm < n && k < n) ? f64_to_f32(gb[u]) : 0.f;
                         }
                     }
 #pragma unroll
@@ -504,7 +504,7 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
 #pragma unroll
                         for (int u = 0; u < 8; ++u) {
                             const int k = 16 * c + kz + u;
-                            z[u] = (L < n && k < n) ? (float)__ldcg(Bs + L + (long long)k * n) : 0.f;
+                            z[u] = (L < n && k < n) ? f64_to_f32(__ldcg(Bs + L + (long long)k * n)) : 0.f;
                         }
                     }
                     c128_put4(st, st + C128_PART, c128_off(L, kz), z[0], z[1], z[2], z[3]);

@@ -59,6 +59,30 @@ __device__ __forceinline__ uint32_t to_tf32(float x)
     return r;
 }
 
+// ---- FP64 -> FP32 conversion on the integer pipes ----
+// GB300's cvt.rn.f32.f64 runs on the FP64 pipe (measured ~2 conversions per
+// clock per SM against ~7.5 for this integer form).  The 128-wide chain
+// kernel, which converts 32K FP64 values per step with registers to spare,
+// uses the bit operations of IEEE round-to-nearest-even (bit-identical to
+// cvt.rn on 268M values spanning the FP32 normal range, ties and carries);
+// in the register-bound 64-wide kernels the longer form measured slower:
+// rebias the exponent (1023 -> 127), keep the top 23 of the 52 fraction bits
+// and round on the other 29 (a carry out of the fraction raises the
+// exponent, as rounding does).  Magnitudes below 2^-126 become signed zero
+// (no FP32 subnormals), above the FP32 range infinity; NaN becomes infinity.
+__device__ __forceinline__ float f64_to_f32(double a)
+{
+    const unsigned hi = (unsigned)__double2hiint(a), lo = (unsigned)__double2loint(a);
+    const unsigned mag = hi & 0x7FFFFFFFu;
+    const int e = (int)(mag >> 20) - 896;
+    unsigned bits = ((unsigned)e << 23) + (((mag & 0xFFFFFu) << 3) | (lo >> 29));
+    const unsigned rest = lo & 0x1FFFFFFFu;
+    bits += (rest > 0x10000000u || (rest == 0x10000000u && (bits & 1u))) ? 1u : 0u;
+    bits = e <= 0 ? 0u : (e >= 255 || bits >= 0x7F800000u ? 0x7F800000u : bits);
+    return __uint_as_float(bits | (hi & 0x80000000u));
+}
+__device__ __forceinline__ float f64_to_f32(float a) { return a; }
+
 // instruction descriptor: kind::tf32, D = F32, A = B = TF32, both K-major,
 // M = 128, N = 128, dense, no negation
 __host__ __device__ constexpr uint32_t tc_idesc_128x128()
