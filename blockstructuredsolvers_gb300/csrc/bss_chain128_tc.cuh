@@ -208,58 +208,100 @@ __device__ __forceinline__ void c128_store_block(float *dst, const float *raw, i
     }
 }
 
-// thread 0: wait for both stages' last commits
-__device__ __forceinline__ void c128_drain(C64Bar (&bar)[2], int *abort)
+// bounded wait for the mbarrier phase of the given parity; sets *abort on expiry
+__device__ __forceinline__ void c128_wait_parity(uint32_t mb, uint32_t parity, int *abort)
 {
-    c64_wait1(bar[0], abort);
-    c64_wait1(bar[1], abort);
+    const long long t0 = clock64();
+    while (!mbar_test(mb, parity))
+        if (clock64() - t0 > C64_WAIT_CYCLES) {
+            *abort = 1;
+            return;
+        }
+}
+
+__device__ __forceinline__ void c128_converters_sync() { asm volatile("bar.sync 2, 224;" ::: "memory"); }
+
+// One product phase (C128_NCHUNK chunks through two stages) with the MMA issue
+// apart from the operand split: warp 0 only issues (tcgen05.mma blocks the
+// issuing thread for the MMA's duration), warps 1-7 split chunk c + 1 into
+// the other stage while the tensor core works on chunk c.  Before that split,
+// thread 32 waits for the MMAs of chunk c - 1 (they read that stage) and, with
+// `ready`, for anything else the split needs; a named barrier then joins the
+// 224 converter threads.  Every phase has 8 chunks, so the commit of chunk c
+// on stage c & 1 completes the mbarrier phase of parity (c >> 1) & 1, and each
+// stage's waits run in order (none waits two phases ahead).  conv(c) runs on
+// the converter threads, issue(c) on thread 0 (its commit follows), after(c)
+// on every thread once chunk c + 1 is split (after(-1): chunk 0).  Returns false (in every thread)
+// when a wait expired; on return every MMA of the phase is complete.
+template <class Ready, class Conv, class Issue, class After>
+__device__ __forceinline__ bool c128_pipeline(const uint32_t (&mb)[2], int *abort, int tid, Ready ready, Conv conv,
+                                              Issue issue, After after)
+{
+    const int w = tid >> 5;
+    // iteration c issues chunk c (c >= 0) and splits chunk c + 1; one call site
+    // each, so the heavy split code is inlined once
+#pragma unroll 1
+    for (int c = -1; c < C128_NCHUNK; ++c) {
+        if (c >= 0 && tid == 0) {
+            tc_fence_after();
+            issue(c);
+            tc_commit(mb[c & 1]);
+        }
+        if (w != 0 && c + 1 < C128_NCHUNK) {
+            if (tid == 32) {
+                if (c >= 1) c128_wait_parity(mb[(c + 1) & 1], (uint32_t)(((c - 1) >> 1) & 1), abort);
+                ready(c + 1);
+            }
+            c128_converters_sync();
+            conv(c + 1);
+            fence_async_smem();  // generic-proxy stores -> visible to the tensor core
+        }
+        tc_fence_before();
+        __syncthreads();
+        if (*abort) return false;
+        after(c);
+    }
+    if (tid == 0) {  // the last commits on both stages: chunks 6 and 7
+        c128_wait_parity(mb[0], (uint32_t)(((C128_NCHUNK - 2) >> 1) & 1), abort);
+        c128_wait_parity(mb[1], (uint32_t)(((C128_NCHUNK - 1) >> 1) & 1), abort);
+    }
+    __syncthreads();
+    tc_fence_after();
+    return *abort == 0;
 }
 
 // phase 1 on the carried rows: D1 = W^T W, D2 = Y^T W, S_LL (+)= Y^T Y.
 // Thread 0 calls rows_read() once the last chunk is split (the carried rows
-// are free; the stages are not, until the drain).  Returns false (in every
-// thread) when a wait expired; on return the products are complete in TMEM.
+// are free; the stages are not, until the phase ends).  Returns false (in
+// every thread) when a wait expired; on return the products are complete in TMEM.
 template <class F>
 __device__ __forceinline__ bool c128_phase1(uint32_t tm, const float *rawW, const float *rawY, unsigned char *stages,
-                                            uint32_t stages_addr, C64Bar (&bar)[2], int *abort, bool sll, int tid,
-                                            F rows_read)
+                                            uint32_t stages_addr, const uint32_t (&mb)[2], int *abort, bool sll,
+                                            int tid, F rows_read)
 {
-    const int rm = tid & 127, rq = tid >> 7;
-#pragma unroll 1
-    for (int c = 0; c < C128_NCHUNK; ++c) {
-        const int s = c & 1;
-        if (tid == 0) c64_wait1(bar[s], abort);  // the MMAs that last read stage s are done
-        tc_fence_before();
-        __syncthreads();
-        if (*abort) return false;
-        unsigned char *st = stages + s * C128_STAGE1;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int q = rq + 2 * h;
-            const uint32_t o = c128_off(rm, 4 * q);
-            const float4 wv = *reinterpret_cast<const float4 *>(rawW + rm * C128_RLD + 16 * c + 4 * q);
-            const float4 yv = *reinterpret_cast<const float4 *>(rawY + rm * C128_RLD + 16 * c + 4 * q);
-            c128_put4(st, st + C128_PART, o, wv.x, wv.y, wv.z, wv.w);
-            c128_put4(st + 2 * C128_PART, st + 3 * C128_PART, o, yv.x, yv.y, yv.z, yv.w);
-        }
-        fence_async_smem();  // generic-proxy stores -> visible to the tensor core
-        __syncthreads();
-        if (tid == 0) {
-            tc_fence_after();
-            const uint32_t a = stages_addr + (uint32_t)(s * C128_STAGE1);
+    return c128_pipeline(
+        mb, abort, tid, [](int) {},
+        [&](int c) {
+            unsigned char *st = stages + (c & 1) * C128_STAGE1;
+            for (int e = tid - 32; e < 512; e += C128_THREADS - 32) {
+                const int m = e & 127, q = e >> 7;
+                const uint32_t o = c128_off(m, 4 * q);
+                const float4 wv = *reinterpret_cast<const float4 *>(rawW + m * C128_RLD + 16 * c + 4 * q);
+                const float4 yv = *reinterpret_cast<const float4 *>(rawY + m * C128_RLD + 16 * c + 4 * q);
+                c128_put4(st, st + C128_PART, o, wv.x, wv.y, wv.z, wv.w);
+                c128_put4(st + 2 * C128_PART, st + 3 * C128_PART, o, yv.x, yv.y, yv.z, yv.w);
+            }
+        },
+        [&](int c) {
+            const uint32_t a = stages_addr + (uint32_t)((c & 1) * C128_STAGE1);
             const uint32_t wh = a, wl = a + C128_PART, yh = a + 2 * C128_PART, yl = a + 3 * C128_PART;
             c128_mma16(tm + C128_T_D1, wh, wl, wh, wl, c > 0);
             c128_mma16(tm + C128_T_D2, yh, yl, wh, wl, c > 0);
             c128_mma16(tm + C128_T_SLL, yh, yl, yh, yl, sll || c > 0);
-            tc_commit(bar[s].addr);
-            bar[s].pending = true;
-            if (c == C128_NCHUNK - 1) rows_read();  // every carried row has been split
-        }
-    }
-    if (tid == 0) c128_drain(bar, abort);
-    __syncthreads();
-    tc_fence_after();
-    return *abort == 0;
+        },
+        [&](int c) {
+            if (c == C128_NCHUNK - 2 && tid == 0) rows_read();  // the last chunk is split: the rows are free
+        });
 }
 
 template <class Tin>
@@ -284,7 +326,6 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
     const int L = 32 * (w & 3) + lane;  // this thread's TMEM lane (accumulator row)
     const int cb = 64 * (w >> 2);       // its first accumulator column
     const uint32_t lane_base = (uint32_t)(32 * (w & 3)) << 16;
-    const int rm = tid & 127, rq = tid >> 7;  // converter mapping: operand row, K group
     const int n = g.n;
     const long long nn = (long long)n * n;
     const bool aligned = ((uintptr_t)g.A_in % 16u) == 0 && ((uintptr_t)g.B_in % 16u) == 0;
@@ -312,8 +353,13 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
     const uint32_t tm = *tslot;
     const uint32_t base_addr = smem_u32(smem_raw);
     const uint32_t mbA = smem_u32(&mbars[2]), mbB = smem_u32(&mbars[2 + C128_NCHUNK]);
-    C64Bar bar[2] = {{smem_u32(&mbars[0]), 0u, false}, {smem_u32(&mbars[1]), 0u, false}};
-    uint32_t a_phase = 0, a_pend = 0, b_phase = 0, b_pend = 0;  // thread 0's view of the copy mbarriers
+    const uint32_t mbs[2] = {smem_u32(&mbars[0]), smem_u32(&mbars[1])};  // stage barriers (MMA commits)
+    // thread 0's view of the stage barriers in phase 2 (phase 1 leaves each
+    // with an even number of completed phases, so the parities agree) and of
+    // the copy mbarriers
+    C64Bar bar[2] = {{mbs[0], 0u, false}, {mbs[1], 0u, false}};
+    uint32_t a_phase = 0, a_pend = 0, b_phase = 0, b_pend = 0;
+    const int rm = tid & 127, rq = tid >> 7;  // phase-2 converter mapping: operand row, K group
 
     // thread 0: A_i column chunk j (16 columns, contiguous) into its buffer
     auto issue_a = [&](const Tin *Ag, int j) {
@@ -365,7 +411,7 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
                     for (int j = 1; j <= 4; ++j) issue_a(Ag, j);
                 }
             };
-            if (!c128_phase1(tm, rawW, rawY, smem_raw + C128_OFF_S1, base_addr + C128_OFF_S1, bar, abort, sll, tid,
+            if (!c128_phase1(tm, rawW, rawY, smem_raw + C128_OFF_S1, base_addr + C128_OFF_S1, mbs, abort, sll, tid,
                              rows_read))
                 break;
             sll = true;
@@ -526,7 +572,10 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
                 if (tmab && c + C128_NBBUF < C128_NCHUNK) issue_b(i, c + C128_NBBUF);
             }
         }
-        if (tid == 0) c128_drain(bar, abort);
+        if (tid == 0) {
+            c64_wait1(bar[0], abort);
+            c64_wait1(bar[1], abort);
+        }
         __syncthreads();
         if (*abort) break;
         tc_fence_after();
@@ -569,7 +618,7 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
 
     // ---- chain end: S_RR = W^T W (D1), S_LR = Y^T W (D2), S_LL += Y^T Y
     if (!*abort && first <= last) {
-        if (c128_phase1(tm, rawW, rawY, smem_raw + C128_OFF_S1, base_addr + C128_OFF_S1, bar, abort, sll, tid,
+        if (c128_phase1(tm, rawW, rawY, smem_raw + C128_OFF_S1, base_addr + C128_OFF_S1, mbs, abort, sll, tid,
                         []() {})) {
             float *Cp = g.C + p * 3 * nn;
 #pragma unroll 1
@@ -594,15 +643,17 @@ __global__ void __launch_bounds__(C128_THREADS, 1)
     }  // partitions
     __syncthreads();
     if (*abort && tid == 0) {
-        // a wait gave up: wait (bounded) for this CTA's MMAs and copies still
-        // in flight before its shared memory and TMEM are released
+        // a wait gave up: wait (bounded) for this CTA's copies in flight and
+        // give its MMAs time to finish before shared memory and TMEM are released
         int ignored = 0;
-        c64_wait1(bar[0], &ignored);
-        c64_wait1(bar[1], &ignored);
         for (int j = 0; j < C128_NCHUNK; ++j) c128_waitbit(mbA + 8u * (uint32_t)j, j, a_phase, a_pend, &ignored);
         for (int b = 0; b < C128_NBBUF; ++b) c128_waitbit(mbB + 8u * (uint32_t)b, b, b_phase, b_pend, &ignored);
+        const long long t0 = clock64();
+        while (clock64() - t0 < C64_WAIT_CYCLES / 8) {
+        }
         if (g.st) atomicExch(&g.st->tc_timeout, 1);
     }
+
     tc_fence_before();
     __syncthreads();
     if (w == 0) {
