@@ -539,7 +539,8 @@ __device__ __noinline__ void inv_column(const T *sS, T *sV, int J, int t0, int n
 // 16-wide panel Cholesky by one warp (as warp_chol_i), the pivot row U(j, :)
 // broadcast through `row` (64 floats of shared memory, double-buffered): one
 // 32-lane store and four 128-bit broadcast reads per pivot instead of up to
-// 15 dependent shuffles
+// 15 dependent shuffles; the one element the next pivot needs, U(j, j+1),
+// comes by a shuffle, so the shared-memory round trip is off the pivot chain
 template <int LD, int PB>
 __device__ __forceinline__ int warp_chol_row(float *sS, float *dinv, float *row, int o, int lane)
 {
@@ -563,16 +564,23 @@ __device__ __forceinline__ int warp_chol_row(float *sS, float *dinv, float *row,
         diag = fmaf(-ujr, ujr, diag);  // own column's diagonal: the pivot chain
         u[j] = ujr;
         if (j + 1 < PB) {
-            float *rj = row + 32 * (j & 1);
-            if (lane < PB) rj[r] = ujr;
-            __syncwarp();
+            // the next pivot needs only U(j, j+1) of this row: one shuffle keeps
+            // it off the shared-memory round trip; the rest of the row (needed
+            // from pivot j + 2 on) goes through shared memory meanwhile
+            const float ujn = __shfl_sync(0xffffffffu, ujr, j + 1);
+            u[j + 1] = fmaf(-ujn, ujr, u[j + 1]);
+            if (j + 2 < PB) {
+                float *rj = row + 32 * (j & 1);
+                if (lane < PB) rj[r] = ujr;
+                __syncwarp();
 #pragma unroll
-            for (int c4 = ((j + 1) / 4) * 4; c4 < PB; c4 += 4) {
-                const float4 v = *reinterpret_cast<const float4 *>(rj + c4);
-                const float ua[4] = {v.x, v.y, v.z, v.w};
+                for (int c4 = ((j + 2) / 4) * 4; c4 < PB; c4 += 4) {
+                    const float4 v = *reinterpret_cast<const float4 *>(rj + c4);
+                    const float ua[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-                for (int t = 0; t < 4; ++t)
-                    if (c4 + t > j) u[c4 + t] = fmaf(-ua[t], ujr, u[c4 + t]);  // S(c, r) -= U(j,c) U(j,r)
+                    for (int t = 0; t < 4; ++t)
+                        if (c4 + t > j + 1) u[c4 + t] = fmaf(-ua[t], ujr, u[c4 + t]);  // S(c, r) -= U(j,c) U(j,r)
+                }
             }
         }
     }
