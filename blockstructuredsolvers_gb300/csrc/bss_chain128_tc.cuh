@@ -44,7 +44,13 @@
 // (stride byte offset 512).  Converter threads take consecutive rows, so
 // each quarter-warp reads and writes 128 contiguous bytes: no bank
 // conflicts.  The chunk after the one being multiplied is split while the
-// tensor core works on the current one.
+// tensor core works on the current one.  tcgen05.mma blocks the issuing
+// thread for the MMA's duration (measured: issue time equals execution
+// time, 104 cycles per M = N = 128, K = 8 TF32 MMA), so phase 1, whose 18
+// MMAs per chunk outweigh its split, is warp-specialised: warp 0 issues
+// chunk c while warps 1-7 split chunk c + 1 (`c128_pipeline`); phase 2,
+// whose split (three operands) outweighs its 12 MMAs, splits on all eight
+// warps and thread 0 issues between barriers.
 //
 // Block loads are bulk copies (cp.async.bulk) completing on mbarriers (L2
 // prefetch hints a step ahead measured no gain in time or DRAM bytes):
@@ -61,11 +67,14 @@
 // Blocks whose columns do not start on 16 bytes (odd n; FP32 input with n
 // not a multiple of 4) are read with plain loads.
 //
-// Thread 0 issues every MMA and is the only thread that waits on the
-// mbarriers (a spin on mbarrier.test_wait bounded by ~1 s of SM clock); the
-// others meet it at the next CTA barrier.  An expired wait sets an abort
-// flag, the CTA stops its chain, thread 0 waits (bounded) for the MMAs still
-// in flight, the CTA frees its TMEM and the timeout is recorded in the status.
+// Thread 0 issues every MMA and waits on the stage barriers at the end of a
+// phase, on the A copies and (phase 2) on the stages and B copies; in phase 1
+// thread 32 waits on the stage barriers for the converter warps.  Every wait
+// is a spin on mbarrier.test_wait bounded by ~1 s of SM clock; the other
+// threads meet the waiting thread at the next barrier.  An expired wait sets
+// an abort flag, the CTA stops its chain, waits (bounded) for its copies and
+// gives its MMAs time to finish, frees its TMEM, and the timeout is recorded
+// in the status.
 #pragma once
 
 namespace bss {
