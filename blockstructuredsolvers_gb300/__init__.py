@@ -25,7 +25,7 @@ from ._lib import BSSError, NotSPDError  # noqa: F401
 
 __all__ = [
     "BlockTriDiagData_batched", "BlockTriDiagData_seq", "initialize_batched", "initialize_seq",
-    "factorize_", "solve_", "factorize", "solve", "synchronize", "get_info", "residual",
+    "factorize_", "solve_", "factorize", "solve", "synchronize", "upload", "download", "get_info", "residual",
     "plan_reference", "BSSError", "NotSPDError", "MultiSystemBatch", "initialize_multi", "Server", "kf_build", "BlockTriDiagData_cpu", "initialize_cpu",
     "ReferenceAlgorithmData", "initialize_reference_algorithm",
     "construct_block_tridiagonal", "SparseCholeskyData", "initialize_sparse_cholesky", "analyze_",
@@ -463,6 +463,71 @@ def solve_(data, check: bool = False) -> None:
 
 factorize = factorize_
 solve = solve_
+
+
+def _host_blocks(X, dims, torch_dtype, what, writable=False):
+    """Address of a dense host array of `count` column-major a x b blocks
+    (dims = (a, b, count)): shape (a, b, count) with column-major strides
+    (Julia's layout) or the same memory as a row-major (count, b, a) array.
+    numpy arrays or CPU torch tensors; nothing is copied."""
+    torch = _torch()
+    import numpy as np
+    a, b, cnt = (int(v) for v in dims)
+    want_f, want_c = (a, b, cnt), (cnt, b, a)
+    if isinstance(X, torch.Tensor):
+        if X.device.type != "cpu":
+            raise ValueError(f"{what}: a host array is required, got a tensor on {X.device}")
+        if X.dtype != torch_dtype:
+            raise ValueError(f"{what}: dtype {X.dtype}, the handle holds {torch_dtype}")
+        shape, st = tuple(X.shape), tuple(X.stride())
+        ok = (shape == want_c and X.is_contiguous()) or (shape == want_f and st == (1, a, a * b))
+        ptr = X.data_ptr()
+    else:
+        if not isinstance(X, np.ndarray):
+            raise ValueError(f"{what}: expected a numpy array or a CPU torch tensor")
+        npdt = np.float64 if torch_dtype == torch.float64 else np.float32
+        if X.dtype != npdt:
+            raise ValueError(f"{what}: dtype {X.dtype}, the handle holds {np.dtype(npdt)}")
+        if writable and not X.flags.writeable:
+            raise ValueError(f"{what}: array is read-only")
+        ok = (X.shape == want_c and X.flags.c_contiguous) or (X.shape == want_f and X.flags.f_contiguous)
+        ptr = X.ctypes.data
+    if not ok:
+        raise ValueError(f"{what}: expected a dense host array of shape {want_f} (column-major) or {want_c} "
+                         f"(row-major), got {tuple(X.shape)}")
+    return ptr
+
+
+def upload(data: _Data, A=None, B=None, d=None, *, upper: bool = False) -> int:
+    """Host arrays -> the handle's A/B/d tensors (bss_upload), the
+    ``copyto!(data.A_tensor, A)`` ... of the reference's callers
+    (benchmark/benchmark_gpu.jl:129-131) for host data.  A: N blocks n x n,
+    B: N-1 blocks, d: N blocks n x k (N the size the handle was created
+    with), column-major (n, n, N) or row-major (N, n, n) host arrays of the
+    handle's dtype; page-locked memory (``tensor.pin_memory()``) makes the
+    copies asynchronous on the handle's stream, and then the arrays must
+    stay alive and unchanged until the stream reaches them.
+
+    ``upper=True``: only the upper triangle of each A_i defines the block
+    (the triangle the reference's potrf(FILL_MODE_UPPER) reads); it is
+    mirrored into the lower one on the device.  Returns the bytes read from
+    host memory."""
+    n, k, N = data.n, data.k, data.N_user
+    pa = _host_blocks(A, (n, n, N), data.dtype, "A") if A is not None else None
+    pb = _host_blocks(B, (n, n, N - 1), data.dtype, "B") if B is not None and N > 1 else None
+    pd = _host_blocks(d, (n, k, N), data.dtype, "d") if d is not None else None
+    moved = ctypes.c_int64()
+    flag = _lib.BSS_UPLOAD_UPPER if upper else _lib.BSS_UPLOAD_FULL
+    _lib.check(_lib.load().bss_upload(data.handle, pa, pb, pd, flag, ctypes.byref(moved)))
+    return moved.value
+
+
+def download(data: _Data, x) -> None:
+    """d_tensor's first N blocks (the solution after solve!) -> host array x
+    (n x k x N, layouts as in upload); asynchronous on the handle's stream
+    when x is page-locked: complete after synchronize(data)."""
+    ptr = _host_blocks(x, (data.n, data.k, data.N_user), data.dtype, "x", writable=True)
+    _lib.check(_lib.load().bss_download(data.handle, ptr))
 
 
 def synchronize(data: _Data) -> None:

@@ -15,6 +15,8 @@ LIB_PATH = os.path.join(HERE, "libbss_gb300.so")
 BSS_OK = 0
 BSS_FACTOR_FMA_CHAIN = 1
 BSS_FACTOR_WIDE_L2 = 2
+BSS_UPLOAD_FULL = 0
+BSS_UPLOAD_UPPER = 1
 BSS_ERR_ARG = 1
 BSS_ERR_OOM = 2
 BSS_ERR_CUDA = 3
@@ -35,7 +37,7 @@ BSS_NOALLOC_SCRATCH_BYTES = 8 << 20
 # every entry point include/bss.h declares
 EXPORTS = (
     "bss_default_options", "bss_create_batched", "bss_create_seq", "bss_destroy",
-    "bss_get_tensors", "bss_get_dims", "bss_factorize", "bss_solve", "bss_synchronize",
+    "bss_get_tensors", "bss_get_dims", "bss_upload", "bss_download", "bss_factorize", "bss_solve", "bss_synchronize",
     "bss_get_info", "bss_last_error_string", "bss_plan_reference", "bss_residual",
     "bss_factorize_levels", "bss_get_level", "bss_factor_solve_noalloc", "bss_kernel_launches",
     "bss_version", "bss_batch_create", "bss_batch_destroy", "bss_batch_get_tensors", "bss_batch_get_dims",
@@ -165,6 +167,8 @@ def load(path: str | None = None):
     L.bss_get_tensors.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]
     L.bss_get_dims.argtypes = [vp, ctypes.POINTER(i64), ctypes.POINTER(i64), ctypes.POINTER(i64),
                                ctypes.POINTER(i32)]
+    L.bss_upload.argtypes = [vp, vp, vp, vp, i32, ctypes.POINTER(i64)]
+    L.bss_download.argtypes = [vp, vp]
     L.bss_factorize.argtypes = [vp]
     L.bss_solve.argtypes = [vp]
     L.bss_synchronize.argtypes = [vp]

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbss_gb300.so")
-SOURCES = ["k_f32.cu", "k_f64.cu", "k_mixed.cu", "bss_api.cu", "bss_noalloc.cu", "bss_batch.cu", "bss_server.cu", "bss_tune.cu", "bss_cpu.cu", "bss_diag.cu", "bss_refalgo.cu", "bss_sparse.cu"]
+SOURCES = ["k_f32.cu", "k_f64.cu", "k_mixed.cu", "bss_api.cu", "bss_upload.cu", "bss_noalloc.cu", "bss_batch.cu", "bss_server.cu", "bss_tune.cu", "bss_cpu.cu", "bss_diag.cu", "bss_refalgo.cu", "bss_sparse.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

@@ -110,6 +110,32 @@ int bss_get_tensors(bss_handle *h, void **A, void **B, void **d);
 /* N_use (the `N` field), n, k and dtype of the handle. */
 int bss_get_dims(bss_handle *h, int64_t *N, int64_t *n, int64_t *k, int32_t *dtype);
 
+/* ---- host upload / download --------------------------------------------------
+ * Replaces the caller's `copyto!(data.A_tensor, A)`, `copyto!(data.B_tensor,
+ * B)`, `copyto!(data.d_tensor, d)` before factorize! (reference
+ * benchmark/benchmark_gpu.jl:129-131) from host arrays, and the read of the
+ * solution out of d_tensor after solve!.  Host arrays hold the N blocks the handle was
+ * created with (not N_use), in the device layout above and the handle's
+ * dtype: A n x n x N, B n x n x (N-1), d (and x) n x k x N, column-major.
+ * The caller guarantees those sizes.  Asynchronous on the handle's stream
+ * when the host memory is page-locked; the padding blocks keep their values.
+ *
+ * flags BSS_UPLOAD_UPPER: only the upper triangle of each A_i defines the
+ * block -- the triangle the reference's potrf(CUBLAS_FILL_MODE_UPPER) reads
+ * (src/backbone_cuda.jl:21-33, 77-99) -- it is mirrored into the lower
+ * triangle on the device, so the host's lower triangles may hold anything.
+ * BSS_UPLOAD_FULL keeps the blocks as copied.  Each tensor is one contiguous
+ * copy.  A, B or d may be NULL (that tensor is left as it is).  *host_bytes
+ * (may be NULL) receives the bytes read from host memory. */
+#define BSS_UPLOAD_FULL 0
+#define BSS_UPLOAD_UPPER 1
+int bss_upload(bss_handle *h, const void *A, const void *B, const void *d, int32_t flags, int64_t *host_bytes);
+
+/* Copies d_tensor's first N blocks (the solution after bss_solve) into host
+ * memory x (n x k x N); asynchronous on the handle's stream: x is complete
+ * after bss_synchronize. */
+int bss_download(bss_handle *h, void *x);
+
 /* Replaces factorize!(data) (gpu_batched.jl:184-227, gpu_seq.jl:61-71).
  * Asynchronous.  Plain precision factors in place like the reference (A and
  * B hold factors afterwards, so it is not idempotent).  Mixed precision keeps
