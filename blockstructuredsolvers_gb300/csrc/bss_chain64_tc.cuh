@@ -37,16 +37,21 @@
 // Block loads: A_{i+1} (into VR, issued once P2 of step i has read V) and
 // B_i (into R's upper half, issued once P1 of step i has read R) are single
 // cp.async.bulk copies completing on mbarriers; both blocks are prefetched
-// into L2 (cp.async.bulk.prefetch.L2) a whole step ahead.  B_i's copy
-// overlaps the Cholesky.  Blocks whose byte size is not a multiple of 16
-// (odd n) are read with plain loads instead.
+// into L2 (cp.async.bulk.prefetch.L2) a whole step ahead.  Blocks whose byte
+// size is not a multiple of 16 (odd n) are read with plain loads instead.
+// Their FP64 -> FP32 conversions run where warps 1-7 would otherwise wait:
+// A_i into the Cholesky tile sS while thread 0 issues P1 and P3, and B_i into
+// its operand rows while warp 0 factors the first diagonal tile of the
+// Cholesky (both in place: every raw value is read into registers before the
+// named barrier 2 lets the first converted one be written).
 //
-// Thread 0 issues every MMA and bulk copy and is the only thread that waits
-// on their mbarriers (a spin on mbarrier.test_wait, bounded by ~1 s of SM
-// clock); the other threads meet it at the next CTA barrier instead of
-// polling.  An expired wait sets an abort flag, the CTA stops its chain,
-// thread 0 waits (bounded) for the copies and MMAs still in flight, the CTA
-// frees its TMEM and the timeout is recorded in the status.
+// Thread 0 issues every MMA and is the only thread that waits on the MMA
+// mbarrier; thread 32 issues the bulk copies and is the only thread that
+// waits on theirs (each a spin on mbarrier.test_wait, bounded by ~1 s of SM
+// clock); the other threads meet them at the next CTA or named barrier
+// instead of polling.  An expired wait sets an abort flag, the CTA stops its
+// chain, threads 0 and 32 wait (bounded) for the MMAs and copies still in
+// flight, the CTA frees its TMEM and the timeout is recorded in the status.
 #pragma once
 
 namespace bss {
@@ -125,6 +130,12 @@ __device__ __forceinline__ void c64_ld32(uint32_t addr, float (&v)[32])
     for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
 }
 
+// warps 1-7 (the converters) meet here; warp 0 never takes part
+__device__ __forceinline__ void c64_workers_sync() { asm volatile("bar.sync 2, 224;" ::: "memory"); }
+
+constexpr int C64_AREG = (64 * 64 + 223) / 224;  // A_i elements per converter thread: 19
+constexpr int C64_BREG = (16 * 64 + 223) / 224;  // B_i 4-element groups per converter thread: 5
+
 template <class Tin>
 __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorArgs<Tin, float> g)
 {
@@ -177,7 +188,7 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
     const uint32_t sRa = smem_u32(R), sVa = smem_u32(VR);
     C64Bar bM{smem_u32(&mbars[0]), 0u, false}, bA{smem_u32(&mbars[1]), 0u, false}, bB{smem_u32(&mbars[2]), 0u, false};
 
-    if (first <= last && bulk && tid == 0) {
+    if (first <= last && bulk && tid == 32) {
         mbar_expect_tx(bA.addr, blk_bytes);
         bulk_g2s(sVa, g.A_in + first * nn, blk_bytes, bA.addr);
         bA.pending = true;
@@ -197,54 +208,61 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
                 sll_started = true;
             }
             c64_wait1(bM, abort);
-            // R has been read: B_i raw into its upper half (it lands during the Cholesky)
-            if (bulk) {
-                fence_async_smem();
-                mbar_expect_tx(bB.addr, blk_bytes);
-                bulk_g2s(sRa + (uint32_t)C64_UPPER, g.B_in + i * nn, blk_bytes, bB.addr);
-                bB.pending = true;
+        } else if (w > 0) {
+            // ---- meanwhile warps 1-7: A_i (identity outside n x n) to FP32 in sS, in place
+            if (tid == 32) {
+                c64_wait1(bA, abort);
+                if (bulk && i < last) {  // the next step's blocks into L2
+                    bulk_prefetch_l2(g.A_in + (i + 1) * nn, blk_bytes);
+                    bulk_prefetch_l2(g.B_in + (i + 1) * nn, blk_bytes);
+                }
             }
-            c64_wait1(bA, abort);
-        }
-        if (tid == 32 && bulk && i < last) {  // the next step's blocks into L2
-            bulk_prefetch_l2(g.A_in + (i + 1) * nn, blk_bytes);
-            bulk_prefetch_l2(g.B_in + (i + 1) * nn, blk_bytes);
+            c64_workers_sync();
+            const Tin *Ag = bulk ? rawA : g.A_in + i * nn;
+            float av[C64_AREG];
+#pragma unroll
+            for (int u = 0; u < C64_AREG; ++u) {
+                const int e = (tid - 32) + 224 * u, r = e & 63, c = e >> 6;
+                av[u] = (e < 4096 && r < n && c < n) ? (float)Ag[r + c * n] : (r == c ? 1.f : 0.f);
+            }
+            c64_workers_sync();  // every raw A_i value is read before sS (same bytes) is written
+#pragma unroll
+            for (int u = 0; u < C64_AREG; ++u) {
+                const int e = (tid - 32) + 224 * u;
+                if (e < 4096) sS[(e & 63) + (e >> 6) * LD] = av[u];
+            }
         }
         __syncthreads();
         if (*abort) break;
+        // R has been read by P1 and P3: B_i raw into its upper half (it lands during the Cholesky)
+        if (tid == 32 && bulk) {
+            fence_async_smem();
+            mbar_expect_tx(bB.addr, blk_bytes);
+            bulk_g2s(sRa + (uint32_t)C64_UPPER, g.B_in + i * nn, blk_bytes, bB.addr);
+            bB.pending = true;
+        }
         tc_fence_after();
-        // ---- Ahat_i (rows L < 64) and Z_i (rows L >= 64) from the P1 accumulator
-        float dv[32];
+        // ---- Ahat_i = A_i - W^T W (rows L < 64) and Z_i (rows L >= 64) from the P1 accumulator
         if (t > 0) {
+            float dv[32];
             c64_ld32(tm + lane_base + (uint32_t)c0, dv);
+            if (L < 64) {
+                if (L < n) {
+#pragma unroll
+                    for (int q = 0; q < 32; ++q)
+                        if (c0 + q < n) sS[L + (c0 + q) * LD] -= dv[q];
+                }
+            } else {
+                const int cz = L - 64;  // column cz of Z = row cz of the P2 operand
+#pragma unroll
+                for (int q = 0; q < 32; q += 4) {
+                    float z[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) z[u] = (cz < n && c0 + q + u < n) ? -dv[q + u] : 0.f;
+                    c64_put4(R, cz, c0 + q, z[0], z[1], z[2], z[3]);
+                }
+            }
         } else {
-#pragma unroll
-            for (int q = 0; q < 32; ++q) dv[q] = 0.f;
-        }
-        if (L < 64) {  // dv <- Ahat row L (identity outside n x n)
-            const Tin *Ag = g.A_in + i * nn;
-#pragma unroll
-            for (int q = 0; q < 32; ++q) {
-                const int c = c0 + q;
-                dv[q] = (L < n && c < n) ? (float)(bulk ? rawA[L + c * n] : Ag[L + (long long)c * n]) - dv[q]
-                                         : (L == c ? 1.f : 0.f);
-            }
-        }
-        __syncthreads();  // every read of the raw A_i is done before sS (same bytes) is written
-        if (L < 64) {
-#pragma unroll
-            for (int q = 0; q < 32; ++q) sS[L + (c0 + q) * LD] = dv[q];
-        } else if (t > 0) {
-            const int cz = L - 64;  // column cz of Z = row cz of the P2 operand
-#pragma unroll
-            for (int q = 0; q < 32; q += 4) {
-                float z[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) z[u] = (cz < n && c0 + q + u < n) ? -dv[q + u] : 0.f;
-                c64_put4(R, cz, c0 + q, z[0], z[1], z[2], z[3]);
-            }
-        }
-        if (t == 0) {
             // Z_first = B_sL^T: row r of the operand (column r of Z) is row r of B_sL
             const int row = tid >> 2, k0 = (tid & 3) * 16;
             const Tin *Bs = g.B_in + sL * nn;
@@ -261,20 +279,61 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
         }
         tc_fence_before();
         __syncthreads();
-        // ---- U^T U = Ahat, V = U^-1 (CUDA cores; ends with a CTA barrier)
-        const int bad = chol_inv_blocked<float, 64, C64_THREADS, true, true>(sS, sV, dinv, sflag, tid, prow);
+        // ---- U^T U = Ahat, V = U^-1 (CUDA cores; ends with a CTA barrier).  While
+        // warp 0 factors the first diagonal tile, warps 1-7 turn the raw B_i in R's
+        // upper half into its operand rows 64-127 (row 64 + j = column j of B_i),
+        // in place: all raw values are read into registers first
+        auto convert_b = [&](int K) {
+            if (K != 0 || !bulk) return;
+            if (tid == 32) c64_wait1(bB, abort);
+            c64_workers_sync();
+            if (*abort) return;
+            float bv[C64_BREG][4];
+#pragma unroll
+            for (int u = 0; u < C64_BREG; ++u) {
+                const int gi = (tid - 32) + 224 * u, j = gi >> 4, k4 = (gi & 15) * 4;
+                if (gi < 1024 && n == 64) {
+                    if constexpr (sizeof(Tin) == 8) {
+                        const double2 b0 = *reinterpret_cast<const double2 *>(rawB + k4 + j * 64);
+                        const double2 b1 = *reinterpret_cast<const double2 *>(rawB + k4 + 2 + j * 64);
+                        bv[u][0] = (float)b0.x;
+                        bv[u][1] = (float)b0.y;
+                        bv[u][2] = (float)b1.x;
+                        bv[u][3] = (float)b1.y;
+                    } else {
+                        const float4 b4 = *reinterpret_cast<const float4 *>(rawB + k4 + j * 64);
+                        bv[u][0] = b4.x;
+                        bv[u][1] = b4.y;
+                        bv[u][2] = b4.z;
+                        bv[u][3] = b4.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int k = k4 + q;
+                        bv[u][q] = (gi < 1024 && j < n && k < n) ? (float)rawB[k + j * n] : 0.f;
+                    }
+                }
+            }
+            c64_workers_sync();  // every raw B_i value is read before its bytes become operand rows
+#pragma unroll
+            for (int u = 0; u < C64_BREG; ++u) {
+                const int gi = (tid - 32) + 224 * u;
+                if (gi < 1024) c64_put4(R, 64 + (gi >> 4), (gi & 15) * 4, bv[u][0], bv[u][1], bv[u][2], bv[u][3]);
+            }
+        };
+        const int bad =
+            chol_inv_blocked<float, 64, C64_THREADS, true, true>(sS, sV, dinv, sflag, tid, prow, convert_b);
         if (bad && tid == 0) record_bad_pivot(g.st, g.level, i);
-        if (tid == 0) c64_wait1(bB, abort);
-        __syncthreads();
         if (*abort) break;
-        // ---- V_i to HBM, and the V_i and B_i operands.  Thread (jr + 16 m, k4):
+        // ---- V_i to HBM and the V_i operand (and, read with plain loads when the
+        // blocks are not bulk-copied, the B_i operand).  Thread (jr + 16 m, k4):
         // 16 threads walk one column's 64 rows in float4 steps (conflict-free
-        // reads of the padded sV and of the raw block, coalesced V stores), and
-        // their operand writes land in distinct bank groups (leading byte offset 144)
+        // reads of the padded sV, coalesced V stores), and their operand writes
+        // land in distinct bank groups (leading byte offset 144)
         {
             const int jr = tid >> 4, k4 = (tid & 15) * 4;
-            float vv[4][4], bv[4][4];
-            const Tin *Bg = g.B_in + i * nn;
+            float vv[4][4];
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
                 const int j = jr + 16 * m;
@@ -284,28 +343,6 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
                 vv[m][1] = lower ? 0.f : v4.y;
                 vv[m][2] = lower ? 0.f : v4.z;
                 vv[m][3] = lower ? 0.f : v4.w;
-                if (bulk && n == 64) {  // 16-byte reads of the raw column
-                    if constexpr (sizeof(Tin) == 8) {
-                        const double2 b0 = *reinterpret_cast<const double2 *>(rawB + k4 + j * 64);
-                        const double2 b1 = *reinterpret_cast<const double2 *>(rawB + k4 + 2 + j * 64);
-                        bv[m][0] = (float)b0.x;
-                        bv[m][1] = (float)b0.y;
-                        bv[m][2] = (float)b1.x;
-                        bv[m][3] = (float)b1.y;
-                    } else {
-                        const float4 b4 = *reinterpret_cast<const float4 *>(rawB + k4 + j * 64);
-                        bv[m][0] = b4.x;
-                        bv[m][1] = b4.y;
-                        bv[m][2] = b4.z;
-                        bv[m][3] = b4.w;
-                    }
-                } else {
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int k = k4 + u;
-                        bv[m][u] = (j < n && k < n) ? (float)(bulk ? rawB[k + j * n] : Bg[k + (long long)j * n]) : 0.f;
-                    }
-                }
             }
             float *Vg = g.A_f + i * nn;
 #pragma unroll
@@ -319,12 +356,21 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
                         if (k4 + u < n) Vg[(long long)j * n + k4 + u] = vv[m][u];
                 }
             }
-            __syncthreads();  // sV and the raw B_i are read: their bytes become operands
+            __syncthreads();  // sV is read: its bytes become the V operand
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
                 const int j = jr + 16 * m;
                 c64_put4(VR, j, k4, vv[m][0], vv[m][1], vv[m][2], vv[m][3]);
-                c64_put4(R, 64 + j, k4, bv[m][0], bv[m][1], bv[m][2], bv[m][3]);
+                if (!bulk) {
+                    const Tin *Bg = g.B_in + i * nn;
+                    float b[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int k = k4 + u;
+                        b[u] = (j < n && k < n) ? (float)Bg[k + (long long)j * n] : 0.f;
+                    }
+                    c64_put4(R, 64 + j, k4, b[0], b[1], b[2], b[3]);
+                }
             }
         }
         fence_async_smem();
@@ -336,17 +382,18 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
             tc_commit(bM.addr);
             bM.pending = true;
             c64_wait1(bM, abort);
-            if (bulk && i < last) {  // V has been read: the next A block into VR
-                fence_async_smem();
-                mbar_expect_tx(bA.addr, blk_bytes);
-                bulk_g2s(sVa, g.A_in + (i + 1) * nn, blk_bytes, bA.addr);
-                bA.pending = true;
-            }
         }
         __syncthreads();
         if (*abort) break;
+        if (tid == 32 && bulk && i < last) {  // P2 has read V: the next A block into VR
+            fence_async_smem();
+            mbar_expect_tx(bA.addr, blk_bytes);
+            bulk_g2s(sVa, g.A_in + (i + 1) * nn, blk_bytes, bA.addr);
+            bA.pending = true;
+        }
         tc_fence_after();
         // ---- Y_i (rows L < 64) and W_i (rows L >= 64): to HBM and into R as [W_i | Y_i]
+        float dv[32];
         c64_ld32(tm + lane_base + (uint32_t)c0, dv);
         {
             const bool isY = L < 64;
@@ -403,14 +450,18 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
         }
     }
     __syncthreads();
-    if (*abort && tid == 0) {
-        // a wait gave up: wait (bounded) for this CTA's copies and MMAs still
-        // in flight before its shared memory and TMEM are released
+    if (*abort) {
+        // a wait gave up: wait (bounded) for this CTA's MMAs (thread 0) and
+        // copies (thread 32) still in flight before its shared memory and
+        // TMEM are released
         int ignored = 0;
-        c64_wait1(bM, &ignored);
-        c64_wait1(bA, &ignored);
-        c64_wait1(bB, &ignored);
-        if (g.st) atomicExch(&g.st->tc_timeout, 1);
+        if (tid == 0) {
+            c64_wait1(bM, &ignored);
+            if (g.st) atomicExch(&g.st->tc_timeout, 1);
+        } else if (tid == 32) {
+            c64_wait1(bA, &ignored);
+            c64_wait1(bB, &ignored);
+        }
     }
     tc_fence_before();
     __syncthreads();

@@ -720,8 +720,16 @@ __device__ __forceinline__ void inv_column_par(float *sS, float *sV, int J, int 
 // FAST (FP32, with INL; `row` = 64 floats of shared memory): the FP32 forms
 // above; the named barrier 1 joins the THREADS - 32 threads that form V's
 // block columns during the panels.
-template <class T, int NB, int THREADS, bool INL = false, bool FAST = false>
-__device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sflag, int tid, T *row = nullptr)
+// `idle(K)` runs on warps 1.. while warp 0 factors diagonal tile K and they
+// have nothing else to do (panel-by-panel order: K < 2 in FP32, every K in
+// FP64): the caller's own work, which must not touch sS, sV or dinv.
+struct CholNoIdle {
+    __device__ __forceinline__ void operator()(int) const {}
+};
+
+template <class T, int NB, int THREADS, bool INL = false, bool FAST = false, class Idle = CholNoIdle>
+__device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sflag, int tid, T *row = nullptr,
+                                                Idle idle = Idle())
 {
     static_assert(!FAST || (INL && sizeof(T) == 4), "the fast forms are inlined FP32");
     static_assert(THREADS > 32, "two warps at least");
@@ -781,6 +789,8 @@ __device__ __forceinline__ int chol_inv_blocked(T *sS, T *sV, T *dinv, int *sfla
                 inv_column_i<T, LD, PB>(sS, sV, K - 1, tid - 32, THREADS - 32);
             else
                 inv_column<T, LD, PB>(sS, sV, K - 1, tid - 32, THREADS - 32);
+        } else {
+            idle(K);
         }
         __syncthreads();
         if (warp == 1) {
