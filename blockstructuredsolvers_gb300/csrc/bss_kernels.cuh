@@ -2528,13 +2528,13 @@ __host__ __device__ constexpr size_t residual_df_smem_cap()
 }
 
 // shared memory of residual_body_df: staged B_i (n (n+1)), x ring (3 nk),
-// u ping-pong (2 nk) and the t / u partials (2 parts nk) as (hi, lo) pairs,
-// plus the FP32 norm partials (25 n); with RAW, the raw FP64 A_i and B_i
-// (16-byte aligned) and their mbarrier
+// u ping-pong (2 nk), d ping-pong (2 nk) and the t / u partials (2 parts nk)
+// as (hi, lo) pairs, plus the FP32 norm partials (25 n); with RAW, the raw
+// FP64 A_i and B_i (16-byte aligned) and their mbarrier
 template <int THREADS, bool RAW = false>
 __host__ __device__ constexpr size_t residual_df_smem_bytes(int n, int k)
 {
-    return ((((size_t)(n * (n + 1) + 5 * n * k + 2 * res_parts<THREADS>(n) * n * k) * 8 + (size_t)25 * n * 4) + 15) /
+    return ((((size_t)(n * (n + 1) + 7 * n * k + 2 * res_parts<THREADS>(n) * n * k) * 8 + (size_t)25 * n * 4) + 15) /
             16 * 16) +
            (RAW ? (size_t)2 * n * n * 8 + 16 : 0);
 }
@@ -2542,6 +2542,12 @@ __host__ __device__ constexpr size_t residual_df_smem_bytes(int n, int k)
 // Same decomposition as residual_body (thread = (row, column part); B_i
 // staged in shared memory for u_{i+1} = B_i^T x_i; x ring and u ping-pong in
 // shared memory), in double-float: shared arrays hold (hi, lo) float pairs.
+// The last phase of a block has three independent jobs -- the outputs r_i,
+// the next block's d (into its ping-pong slot) and x_{i+2} (into the ring) --
+// and a CTA has more threads than n k outputs when k is small, so each job
+// starts at a different quarter of the CTA (for k = 1, n = 64 on 256 threads:
+// two warps each), and the norm partials at the fourth: their global-memory
+// latencies overlap instead of queueing on the output threads.
 // Shared memory: residual_df_smem_bytes<THREADS, RAW>(n, k).
 // RAW (even n, 16-byte-aligned A and B): each block's FP64 A_i and B_i come
 // into shared memory by bulk copies (cp.async.bulk on an mbarrier), the next
@@ -2562,8 +2568,9 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
     float2 *sB = reinterpret_cast<float2 *>(smem_raw);
     float2 *sxr = sB + n * LDp;      // [3][nk]
     float2 *sub = sxr + 3 * nk;      // [2][nk] u_i ping-pong
+    float2 *sdd = sub + 2 * nk;      // [2][nk] d_i ping-pong (split)
     const int parts = res_parts<THREADS>(n);
-    float2 *red = sub + 2 * nk;      // [2][parts][nk]
+    float2 *red = sdd + 2 * nk;      // [2][parts][nk]
     float2 *redu = red + parts * nk;  // u partials
     float *rowred = reinterpret_cast<float *>(red + 2 * parts * nk);  // [3][8][n]
     float *rowu = rowred + 24 * n;   // [n]
@@ -2603,8 +2610,12 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
     float rmax = 0.0f, xmax = 0.0f, amax = 0.0f;
     auto xs = [&](long long blk) { return sxr + (int)((blk - b0 + 3) % 3) * nk; };  // blk in [b0-1, b1]
 
-    // prologue: x_{b0-1}, x_{b0}, x_{b0+1}; u_{b0} = B_{b0-1}^T x_{b0-1}
+    // the first thread of a job that starts at quarter s of the CTA
+    const int T = blockDim.x;
+    auto rot = [&](int q4) { return (tid + T - (q4 * T) / 4) % T; };
+    // prologue: x_{b0-1}, x_{b0}, x_{b0+1}, d_{b0}; u_{b0} = B_{b0-1}^T x_{b0-1}
     for (int e = tid; e < nk; e += blockDim.x) {
+        sdd[e] = split_df(d[b0 * bstride + coff + e]);
         xs(b0)[e] = split_df(x[b0 * bstride + coff + e]);
         if (b0 + 1 < N) xs(b0 + 1)[e] = split_df(x[(b0 + 1) * bstride + coff + e]);
         sub[e] = make_float2(0.0f, 0.0f);
@@ -2711,10 +2722,11 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
             }
         }
         __syncthreads();
-        // phase 3: r_i = d_i - t - u_i; fetch x_{i+2}
+        // phase 3: r_i = d_i - t - u_i; fetch d_{i+1} and x_{i+2}
+        const float2 *sd = sdd + par * nk;
         for (int o = tid; o < nk; o += blockDim.x) {
             const int j = o / n, rr = o - j * n;
-            const float2 dd = split_df(d[i * bstride + coff + o]);
+            const float2 dd = sd[o];
             float rh = dd.x, rl = dd.y;
             float uh = 0.0f, ul = 0.0f;
             for (int q = 0; q < parts; ++q) {
@@ -2740,8 +2752,12 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
             xmax = fmaxf(xmax, fabsf(x0[o].x));
             sun[o] = make_float2(uh, ul);
         }
+        if (i + 1 < b1) {
+            float2 *sdn = sdd + (par ^ 1) * nk;
+            for (int e = rot(1); e < nk; e += T) sdn[e] = split_df(d[(i + 1) * bstride + coff + e]);
+        }
         if (with_norm)
-            for (int rr = tid; rr < n; rr += blockDim.x) {
+            for (int rr = rot(3); rr < n; rr += T) {
                 float s = rowu[rr], s2 = 0.0f;
                 for (int q = 0; q < parts; ++q) {
                     s += rowred[q * n + rr];
@@ -2752,7 +2768,7 @@ __device__ __forceinline__ void residual_body_df(const double *__restrict__ A, c
             }
         if (i + 2 < N && i + 1 < b1) {
             float2 *x2 = xs(i + 2);
-            for (int e = tid; e < nk; e += blockDim.x) x2[e] = split_df(x[(i + 2) * bstride + coff + e]);
+            for (int e = rot(2); e < nk; e += T) x2[e] = split_df(x[(i + 2) * bstride + coff + e]);
         }
         __syncthreads();
     }
