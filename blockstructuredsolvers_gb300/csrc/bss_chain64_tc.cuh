@@ -5,16 +5,20 @@
 // the block loads on the bulk-copy (TMA) engine.
 //
 // Products (K = 64, 3xTF32: x = hi + lo, C = Xh Yh + Xh Yl + Xl Yh in the FP32
-// TMEM accumulator, relative error ~2^-21 like FP32 FMA products).  Each is one
-// M = 128, N = 64 MMA sequence whose A operand stacks two 64-row operands:
-//   P1 = [W_{i-1} | Y_{i-1}]^T W_{i-1}   rows 0-63:   W^T W       -> Ahat_i = A_i - W^T W
-//                                          rows 64-127: Y^T W       -> Z_i = -(Y^T W)^T
-//   P3 = [W_{i-1} | Y_{i-1}]^T Y_{i-1}   rows 64-127: Y^T Y, accumulated in TMEM
-//                                          over the chain (S_LL); rows 0-63 unused
-//   P2 = [Z_i | B_i]^T V_i                rows 0-63:   Z^T V = Y_i^T
-//                                          rows 64-127: B^T V = W_i^T
+// TMEM accumulator, relative error ~2^-21 like FP32 FMA products).  The A
+// operand of each stacks two 64-row operands (M = 128):
+//   P1 = [W_{i-1} | Y_{i-1}]^T [W_{i-1} | Y_{i-1}]   (N = 128)
+//        columns 0-63,   rows 0-63:   W^T W  -> Ahat_i = A_i - W^T W
+//        columns 0-63,   rows 64-127: Y^T W  -> Z_i = -(Y^T W)^T
+//        columns 64-127, rows 64-127: Y^T Y, accumulated in TMEM over the
+//        chain (S_LL); rows 0-63 unused
+//   P2 = [Z_i | B_i]^T V_i                   (N = 64)
+//        rows 0-63:   Z^T V = Y_i^T
+//        rows 64-127: B^T V = W_i^T
 // and at the chain end P1 on [W_last | Y_last] gives S_RR = W^T W and
-// S_LR = Y^T W.  Reference: the potrf/trsm/gemm sequence of
+// S_LR = Y^T W with the last S_LL term.  P1 accumulates onto all 128
+// columns (one MMA sequence cannot overwrite some columns and accumulate
+// others), so the readout of P2 stores zeros into columns 0-63 behind it.  Reference: the potrf/trsm/gemm sequence of
 // cholesky_factorize_batched! and the Schur products of
 // compute_schur_complement! (src/backbone_cuda.jl:70-101, 143-157).
 //
@@ -32,7 +36,7 @@
 //   VR  36 KB  the Cholesky tiles sS, sV (padded column-major, as
 //              chol_inv_blocked wants them); after the Cholesky the V operand
 //              (same layout); between steps the raw A_{i+1}
-// TMEM: 128 columns: 0-63 the P1/P2 accumulator, 64-127 S_LL.
+// TMEM: 128 columns: 0-63 the P1/P2 accumulator, 64-127 S_LL (P1's second half).
 //
 // Block loads: A_{i+1} (into VR, issued once P2 of step i has read V) and
 // B_i (into R's upper half, issued once P1 of step i has read R) are single
@@ -40,7 +44,7 @@
 // into L2 (cp.async.bulk.prefetch.L2) a whole step ahead.  Blocks whose byte
 // size is not a multiple of 16 (odd n) are read with plain loads instead.
 // Their FP64 -> FP32 conversions run where warps 1-7 would otherwise wait:
-// A_i into the Cholesky tile sS while thread 0 issues P1 and P3, and B_i into
+// A_i into the Cholesky tile sS while thread 0 issues P1, and B_i into
 // its operand rows while warp 0 factors the first diagonal tile of the
 // Cholesky (both in place: every raw value is read into registers before the
 // named barrier 2 lets the first converted one be written).
@@ -86,6 +90,12 @@ __host__ __device__ constexpr uint32_t c64_idesc()
     return (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
 }
 
+// kind::tf32, D = F32, A = B = TF32, both K-major, M = 128, N = 128
+__host__ __device__ constexpr uint32_t c64_idesc_n128()
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+}
+
 // TMEM cols at tm (+)= Aop(128 rows at shared address a) x Bop(64 rows at b)^T
 // over K = 64 in 3xTF32; issued by one thread
 __device__ __forceinline__ void c64_mma(uint32_t tm, uint32_t a, uint32_t b, bool accumulate)
@@ -100,6 +110,31 @@ __device__ __forceinline__ void c64_mma(uint32_t tm, uint32_t a, uint32_t b, boo
         tc_mma(tm, ah, bl, id, 1u);
         tc_mma(tm, al, bh, id, 1u);
     }
+}
+
+// TMEM cols tm .. tm+127 (+)= R x R^T over K = 64 in 3xTF32 (R: the 128 stacked
+// operand rows at shared address r, as both A and B); issued by one thread
+__device__ __forceinline__ void c64_mma_rr(uint32_t tm, uint32_t r, bool accumulate)
+{
+    constexpr uint32_t id = c64_idesc_n128();
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+        const uint32_t o = (uint32_t)kk * (2u * C64_LBO);
+        const uint64_t h = c64_desc(r + o), l = c64_desc(r + C64_PART + o);
+        tc_mma(tm, h, h, id, (accumulate || kk) ? 1u : 0u);
+        tc_mma(tm, h, l, id, 1u);
+        tc_mma(tm, l, h, id, 1u);
+    }
+}
+
+// zeros into 32 consecutive accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void c64_zero32(uint32_t addr)
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,"
+        "%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(addr), "r"(0u)
+        : "memory");
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
 // four consecutive K values (k4 .. k4+3) of one operand row, split hi / lo
@@ -198,11 +233,10 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
     for (long long i = first; i <= last; ++i) {
         const long long t = i - first;
         if (tid == 0) {
-            // ---- P1 and P3 on [W_{i-1} | Y_{i-1}] (written and fenced by the previous step)
+            // ---- P1 on [W_{i-1} | Y_{i-1}] (written and fenced by the previous step)
             if (t > 0) {
                 tc_fence_after();
-                c64_mma(tm, sRa, sRa, false);
-                c64_mma(tm + 64u, sRa, sRa + (uint32_t)C64_UPPER, sll_started);
+                c64_mma_rr(tm, sRa, sll_started);
                 tc_commit(bM.addr);
                 bM.pending = true;
                 sll_started = true;
@@ -234,7 +268,7 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
         }
         __syncthreads();
         if (*abort) break;
-        // R has been read by P1 and P3: B_i raw into its upper half (it lands during the Cholesky)
+        // R has been read by P1: B_i raw into its upper half (it lands during the Cholesky)
         if (tid == 32 && bulk) {
             fence_async_smem();
             mbar_expect_tx(bB.addr, blk_bytes);
@@ -395,6 +429,7 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
         // ---- Y_i (rows L < 64) and W_i (rows L >= 64): to HBM and into R as [W_i | Y_i]
         float dv[32];
         c64_ld32(tm + lane_base + (uint32_t)c0, dv);
+        c64_zero32(tm + lane_base + (uint32_t)c0);  // the next P1 accumulates onto these columns
         {
             const bool isY = L < 64;
             const int col = isY ? L : L - 64;
@@ -417,12 +452,11 @@ __global__ void __launch_bounds__(C64_THREADS, 2) chain64_tc_kernel(ChainFactorA
         __syncthreads();
     }
 
-    // ---- chain end: S_RR = W^T W, S_LR = Y^T W (P1) and the last S_LL term (P3)
+    // ---- chain end: S_RR = W^T W, S_LR = Y^T W and the last S_LL term (P1)
     if (!*abort && first <= last) {
         if (tid == 0) {
             tc_fence_after();
-            c64_mma(tm, sRa, sRa, false);
-            c64_mma(tm + 64u, sRa, sRa + (uint32_t)C64_UPPER, sll_started);
+            c64_mma_rr(tm, sRa, sll_started);
             tc_commit(bM.addr);
             bM.pending = true;
             c64_wait1(bM, abort);
