@@ -585,10 +585,11 @@ def run_ours(args):
 
     # ---- e2e through the public API with host buffers ----------------------
     # A stream of requests, each: pinned host A, B, d -> device (bss.upload),
-    # factorize!, solve!, x -> pinned host (bss.download).  Two handles on two
-    # CUDA streams take alternate requests (the double buffering a serving
-    # caller uses), so one request's copies overlap the other's compute; every
-    # request still pays its own H2D and D2H inside the timed region.  The
+    # factorize!, solve!, x -> pinned host (bss.download).  Three handles on
+    # three CUDA streams take requests in turn (the buffering a serving caller
+    # uses), so one request's copies overlap another's compute; every request
+    # still pays its own H2D and D2H inside the timed region.  (Two handles
+    # reach the same rate once warm, three absorb the jitter of the copies.)  The
     # host link bounds it: the copy engines' rate from pinned host memory is
     # measured beside it (one whole-buffer copy), with the solves/s that rate
     # allows for these bytes; the one-handle serial figure is reported too.
@@ -598,7 +599,7 @@ def run_ours(args):
         Ah = torch.from_numpy(As).pin_memory()
         Bh = torch.from_numpy(Bs).pin_memory()
         dh = torch.from_numpy(ds).pin_memory()
-        streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+        streams = [torch.cuda.Stream() for _ in range(3)]
         slots = []
         for st in streams:
             with torch.cuda.stream(st):
@@ -625,6 +626,7 @@ def run_ours(args):
         for slot in slots:  # first calls run eagerly and capture the graphs
             for _ in range(2):
                 e2e_step(slot)
+        e2e_run(len(slots) * 2, slots)  # the copies and the pipeline warm
         te = e2e_run(ne, slots)
         bi = moved[0]
         n1 = max(5, ne // 2)
@@ -644,7 +646,7 @@ def run_ours(args):
         link_gbs = 3 * Bh.numel() * 8 / (lk0.elapsed_time(lk1) * 1e-3) / 1e9
         e2e = {"value": world * ne / te, "unit": "solves/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
                "requests_timed": ne,
-               "mode": "two handles on two streams, alternate requests, copies inside the timed region; "
+               "mode": "three handles on three streams, requests in turn, copies inside the timed region; "
                        "bss.upload / bss.download",
                "serial_one_handle": world / te1, "rel_residual_last_x": rr_e2e,
                "rel_error_vs_oracle_last_x": rel_err_stor(slots[0][2].numpy(), x_ref) if rank == 0 else None,
