@@ -525,65 +525,8 @@ def run_ours(args):
     d = torch.from_numpy(ds).to(dev).permute(2, 1, 0)
     hbm, peak_kind = hbm_peak()
     peaks = fma_peaks()
-    # ---- headline: mixed precision, inputs resident in HBM -------------------
-    sampler = ClockSampler(local)
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    launches0 = L.bss_kernel_launches()
-    sampler.start()
-    secs, fac, sol, data = time_leg(bss, A, B, d, torch.float64, "mixed", args.steps, args.warmup, False)
-    clocks = sampler.stop()
-    launches = L.bss_kernel_launches() - launches0
-    info = bss.get_info(data)
-    x = data.d_tensor[:, :, :N_BLK]
-    relres = rel_residual_dev(A, B, x, d)
-    x_head = x.permute(2, 1, 0).contiguous().cpu().numpy()  # (N, k, n): the oracle's storage order
-    del data, x
-    # the warmup steps launched too: count per step from the total
-    launches_per_step = launches / max(args.steps + args.warmup, 1)
-    from blockstructuredsolvers_gb300 import replicas
-    secs = replicas.reduce_max(secs)  # the slowest replica's time
-    value = world * args.steps / secs
-    x_ref = oracle_x(As, Bs, ds) if rank == 0 else None
-    err_head = rel_err_stor(x_head, x_ref) if rank == 0 else None
-    cfg1 = [(N_BLK, N_SZ, K_RHS)]
-    head_roof = leg_roofline(cfg1, 8, statistics.median(fac), statistics.median(sol), peaks["f32"], "FP32", hbm)
-
-    extra = {"peaks_measured": {"fp64_fma_tflops": peaks["f64"], "fp32_fma_tflops": peaks["f32"],
-                                "hbm_gbs": hbm, "hbm_source": f"MEASURED_PEAKS.json ({peak_kind})"}}
-    if not args.quick:
-        # ---- plain FP64 and plain FP32 GPU paths (same request) ---------------
-        n64 = max(3, args.steps // 4)
-        s64, f64, so64, d64 = time_leg(bss, A, B, d, torch.float64, "plain", n64, 1, True)
-        rr64 = rel_residual_dev(A, B, d64.d_tensor[:, :, :N_BLK], d)
-        x64 = d64.d_tensor[:, :, :N_BLK].permute(2, 1, 0).contiguous().cpu().numpy()
-        del d64
-        s32, f32, so32, d32 = time_leg(bss, A, B, d, torch.float32, "plain", n64, 1, True)
-        rr32 = rel_residual_dev(A.float().double(), B.float().double(), d32.d_tensor[:, :, :N_BLK].double(),
-                                d.float().double())
-        x32 = d32.d_tensor[:, :, :N_BLK].permute(2, 1, 0).double().contiguous().cpu().numpy()
-        del d32
-        extra["autotuned"] = run_autotuned(bss, A, B, d)
-        extra["reference_algorithm_gpu"] = time_reference_algorithm(bss, A, B, d)
-        extra["sparse_cholesky_gpu"] = time_sparse_cholesky(bss, A, B, d, hbm)
-        extra["k16"] = run_k16(bss, A, B, dev, peaks, hbm, rank == 0)
-        fm64, sm64 = statistics.median(f64), statistics.median(so64)
-        extra["plain_fp64"] = {"solves_per_s": n64 / s64, "factor_ms": fm64, "solve_ms": sm64,
-                               "rel_residual": rr64,
-                               "rel_error_vs_oracle": rel_err_stor(x64, x_ref) if rank == 0 else None,
-                               "refine_steps": 0,
-                               "roofline": leg_roofline(cfg1, 8, fm64, sm64, peaks["f64"], "FP64", hbm),
-                               "note": "solves/s includes the device copy of A, B, d into the handle per step"}
-        fm32, sm32 = statistics.median(f32), statistics.median(so32)
-        extra["plain_fp32"] = {"solves_per_s": n64 / s32, "factor_ms": fm32, "solve_ms": sm32,
-                               "rel_residual_fp32_system": rr32,
-                               "rel_error_vs_oracle": rel_err_stor(x32, x_ref) if rank == 0 else None,
-                               "refine_steps": 0,
-                               "roofline": leg_roofline(cfg1, 4, fm32, sm32, peaks["f32"], "FP32", hbm),
-                               "note": "FP32 accuracy only; not a rel-resid <= 1e-12 result"}
-
     # ---- e2e through the public API with host buffers ----------------------
+    # (first of the legs: measured in a process that has not yet run the others)
     # A stream of requests, each: pinned host A, B, d -> device (bss.upload),
     # factorize!, solve!, x -> pinned host (bss.download).  Three handles on
     # three CUDA streams take requests in turn (the buffering a serving caller
@@ -626,7 +569,10 @@ def run_ours(args):
         for slot in slots:  # first calls run eagerly and capture the graphs
             for _ in range(2):
                 e2e_step(slot)
-        e2e_run(len(slots) * 2, slots)  # the copies and the pipeline warm
+        # host-to-device copies reach the link's full rate only after ~0.3 s of
+        # sustained transfers (the first 50 requests after an idle pause ran at
+        # 140 - 180 solves/s, the next 50 at 192.5): warm the pipeline first
+        e2e_run(max(60, ne), slots)
         te = e2e_run(ne, slots)
         bi = moved[0]
         n1 = max(5, ne // 2)
@@ -649,10 +595,71 @@ def run_ours(args):
                "mode": "three handles on three streams, requests in turn, copies inside the timed region; "
                        "bss.upload / bss.download",
                "serial_one_handle": world / te1, "rel_residual_last_x": rr_e2e,
-               "rel_error_vs_oracle_last_x": rel_err_stor(slots[0][2].numpy(), x_ref) if rank == 0 else None,
+               "rel_error_vs_oracle_last_x": None,
                "link": {"h2d_gbs": link_gbs, "bound_solves_per_s": world * link_gbs * 1e9 / bi,
                         "note": "one pinned copy engine transfer of B, timed on the device"}}
+        x_e2e_host = slots[0][2].numpy().copy()
         del slots
+
+    # ---- headline: mixed precision, inputs resident in HBM -------------------
+    sampler = ClockSampler(local)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = L.bss_kernel_launches()
+    sampler.start()
+    secs, fac, sol, data = time_leg(bss, A, B, d, torch.float64, "mixed", args.steps, args.warmup, False)
+    clocks = sampler.stop()
+    launches = L.bss_kernel_launches() - launches0
+    info = bss.get_info(data)
+    x = data.d_tensor[:, :, :N_BLK]
+    relres = rel_residual_dev(A, B, x, d)
+    x_head = x.permute(2, 1, 0).contiguous().cpu().numpy()  # (N, k, n): the oracle's storage order
+    del data, x
+    # the warmup steps launched too: count per step from the total
+    launches_per_step = launches / max(args.steps + args.warmup, 1)
+    from blockstructuredsolvers_gb300 import replicas
+    secs = replicas.reduce_max(secs)  # the slowest replica's time
+    value = world * args.steps / secs
+    x_ref = oracle_x(As, Bs, ds) if rank == 0 else None
+    if e2e is not None and rank == 0:
+        e2e["rel_error_vs_oracle_last_x"] = rel_err_stor(x_e2e_host, x_ref)
+    err_head = rel_err_stor(x_head, x_ref) if rank == 0 else None
+    cfg1 = [(N_BLK, N_SZ, K_RHS)]
+    head_roof = leg_roofline(cfg1, 8, statistics.median(fac), statistics.median(sol), peaks["f32"], "FP32", hbm)
+
+    extra = {"peaks_measured": {"fp64_fma_tflops": peaks["f64"], "fp32_fma_tflops": peaks["f32"],
+                                "hbm_gbs": hbm, "hbm_source": f"MEASURED_PEAKS.json ({peak_kind})"}}
+    if not args.quick:
+        # ---- plain FP64 and plain FP32 GPU paths (same request) ---------------
+        n64 = max(3, args.steps // 4)
+        s64, f64, so64, d64 = time_leg(bss, A, B, d, torch.float64, "plain", n64, 1, True)
+        rr64 = rel_residual_dev(A, B, d64.d_tensor[:, :, :N_BLK], d)
+        x64 = d64.d_tensor[:, :, :N_BLK].permute(2, 1, 0).contiguous().cpu().numpy()
+        del d64
+        s32, f32, so32, d32 = time_leg(bss, A, B, d, torch.float32, "plain", n64, 1, True)
+        rr32 = rel_residual_dev(A.float().double(), B.float().double(), d32.d_tensor[:, :, :N_BLK].double(),
+                                d.float().double())
+        x32 = d32.d_tensor[:, :, :N_BLK].permute(2, 1, 0).double().contiguous().cpu().numpy()
+        del d32
+        extra["autotuned"] = run_autotuned(bss, A, B, d)
+        extra["reference_algorithm_gpu"] = time_reference_algorithm(bss, A, B, d)
+        extra["sparse_cholesky_gpu"] = time_sparse_cholesky(bss, A, B, d, hbm)
+        extra["k16"] = run_k16(bss, A, B, dev, peaks, hbm, rank == 0)
+        fm64, sm64 = statistics.median(f64), statistics.median(so64)
+        extra["plain_fp64"] = {"solves_per_s": n64 / s64, "factor_ms": fm64, "solve_ms": sm64,
+                               "rel_residual": rr64,
+                               "rel_error_vs_oracle": rel_err_stor(x64, x_ref) if rank == 0 else None,
+                               "refine_steps": 0,
+                               "roofline": leg_roofline(cfg1, 8, fm64, sm64, peaks["f64"], "FP64", hbm),
+                               "note": "solves/s includes the device copy of A, B, d into the handle per step"}
+        fm32, sm32 = statistics.median(f32), statistics.median(so32)
+        extra["plain_fp32"] = {"solves_per_s": n64 / s32, "factor_ms": fm32, "solve_ms": sm32,
+                               "rel_residual_fp32_system": rr32,
+                               "rel_error_vs_oracle": rel_err_stor(x32, x_ref) if rank == 0 else None,
+                               "refine_steps": 0,
+                               "roofline": leg_roofline(cfg1, 4, fm32, sm32, peaks["f32"], "FP32", hbm),
+                               "note": "FP32 accuracy only; not a rel-resid <= 1e-12 result"}
 
     # ---- roofline of the dominant kernel ----------------------------------
     roof = roofline_chain_factor(bss, A, B, d, hbm, peak_kind)
