@@ -1916,11 +1916,11 @@ __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long
         last = sR - 1;
     }
     for (int e = threadIdx.x; e < nkc; e += blockDim.x) sbL[e] = T(0);
-    // step i uses V_i (slot 0), W_{i-1} (slot 1), Y_i (slot 2) and d_i in buffer (i - first) & 1
-    if (STAGED) {
-        async_copy(buf, g.Af + first * (long long)nn, nn);
-        if (!seq) async_copy(buf + 2 * nn, g.Y + first * (long long)nn, nn);
-    }
+    // step i uses V_i (slot 0), W_{i-1} (slot 1), Y_{i-1} (slot 2) and d_i in buffer
+    // (i - first) & 1: the products with W_{i-1} (into this step's RHS) and Y_{i-1}
+    // (into bL) both read y_{i-1}, so they share the step's first phase, and y_{i-1}
+    // is stored there too; the step's second phase is y_i = V_i^T r_i
+    if (STAGED) async_copy(buf, g.Af + first * (long long)nn, nn);
     async_copy(srb, rhs_ptr<T>(g.d, first, n, g.k, g.j0), nkc);
     cp_async_commit();
     for (long long i = first; i <= last; ++i) {
@@ -1930,38 +1930,42 @@ __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long
         T *sr = srb + cb * nkc;
         cp_async_wait_all();
         __syncthreads();
-        // prefetch step i+1 (W_i is also what bR needs after the last step)
+        // prefetch step i+1: V_{i+1} and d_{i+1}, and W_i, Y_i for its first phase
+        // (after the last step, W_last and Y_last for bR and the last bL term)
         if (i < last) {
             if (STAGED) async_copy(nxt, g.Af + (i + 1) * (long long)nn, nn);
             async_copy(srb + (cb ^ 1) * nkc, rhs_ptr<T>(g.d, i + 1, n, g.k, g.j0), nkc);
         }
         if (STAGED && (!seq || i < last)) async_copy(nxt + nn, g.Bf + i * (long long)nn, nn);
-        if (STAGED && !seq && i < last) async_copy(nxt + 2 * nn, g.Y + (i + 1) * (long long)nn, nn);
+        if (STAGED && !seq) async_copy(nxt + 2 * nn, g.Y + i * (long long)nn, nn);
         cp_async_commit();
         // matrices of step i: staged in shared memory, or read straight from global
         // memory (then the next step's are hinted into L2 while this one runs)
         if (!STAGED && i < last) {
             prefetch_l2(g.Af + (i + 1) * (long long)nn, (size_t)nn * sizeof(T));
             prefetch_l2(g.Bf + i * (long long)nn, (size_t)nn * sizeof(T));
-            if (!seq) prefetch_l2(g.Y + (i + 1) * (long long)nn, (size_t)nn * sizeof(T));
+            if (!seq) prefetch_l2(g.Y + i * (long long)nn, (size_t)nn * sizeof(T));
         }
         const T *mV = STAGED ? cur : g.Af + i * (long long)nn;
-        const T *mW = STAGED ? cur + nn : g.Bf + (i - 1) * (long long)nn;
-        const T *mY = STAGED ? cur + 2 * nn : g.Y + i * (long long)nn;
         if (i > first) {
+            const T *mW = STAGED ? cur + nn : g.Bf + (i - 1) * (long long)nn;
+            const T *mY = STAGED ? cur + 2 * nn : g.Y + (i - 1) * (long long)nn;
+            store_rhs(g.d, sy, i - 1, n, g.k, g.j0, kc);
             tmul<STAGED>(mW, sy, sr, n, kc, T(-1), true);
+            if (!seq) tmul<STAGED>(mY, sy, sbL, n, kc, T(1), true);
             __syncthreads();
         }
         tmul<STAGED>(mV, sr, sy, n, kc, T(1), false);
-        __syncthreads();
-        if (!seq) tmul<STAGED>(mY, sy, sbL, n, kc, T(1), true);
-        store_rhs(g.d, sy, i, n, g.k, g.j0, kc);
     }
     cp_async_wait_all();
     __syncthreads();
+    store_rhs(g.d, sy, last, n, g.k, g.j0, kc);
     if (!seq) {
-        const T *wl = STAGED ? buf + (((last + 1 - first) & 1) * 3 + 1) * nn  // W_last, prefetched in the last step
-                             : g.Bf + last * (long long)nn;
+        // bL += Y_last^T y_last, bR = W_last^T y_last (both prefetched in the last step)
+        const T *nb = buf + ((last + 1 - first) & 1) * 3 * nn;
+        const T *wl = STAGED ? nb + nn : g.Bf + last * (long long)nn;
+        const T *yl = STAGED ? nb + 2 * nn : g.Y + last * (long long)nn;
+        tmul<STAGED>(yl, sy, sbL, n, kc, T(1), true);
         tmul<STAGED>(wl, sy, sbR, n, kc, T(1), false);
         __syncthreads();
         T *bp = g.bvec + p * 2 * (long long)nkc;
@@ -1971,6 +1975,7 @@ __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long
         }
         return;
     }
+    __syncthreads();  // every y_i is stored before the backward sweep reads them back
     // sequential level, backward: x_i = V_i (y_i - W_i x_{i+1}); step i uses
     // V_i (slot 0), W_i (slot 1) and y_i
     if (STAGED) async_copy(buf, g.Af + last * (long long)nn, nn);
@@ -2009,13 +2014,13 @@ __device__ __forceinline__ void chain_fwd_body(const SolveArgs<T> &g, const long
 }
 
 template <class T, bool STAGED>
-__global__ void __launch_bounds__(SOLVE_THREADS) chain_fwd_kernel(SolveArgs<T> g)
+__global__ void __launch_bounds__(SOLVE_THREADS, 2) chain_fwd_kernel(SolveArgs<T> g)
 {
     chain_fwd_body<T, STAGED>(g, blockIdx.x);
 }
 
 template <class T, bool STAGED>
-__global__ void __launch_bounds__(SOLVE_THREADS)
+__global__ void __launch_bounds__(SOLVE_THREADS, 2)
     chain_fwd_queue_kernel(const SolveArgs<T> *__restrict__ descs, const WorkItem *__restrict__ items, int nitems,
                            int *head)
 {
